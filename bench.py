@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark: RPY M.f applies per right-hand side, reported as ns per particle
+per right-hand side (lower is better), FP32-batched operator on one GB300.
+
+Workload (default "large"): N = 1e6 particles uniform in a periodic box
+L = 480, radius a = 1, xi = 0.3, rc = 10, mesh K = 256, B-spline order p = 6,
+R = 16 right-hand sides i.i.d. N(0,1).  A step is one drop-in style apply
+with new positions: positions -> B-spline records + tile sort + cell list,
+then M = M_recip + M_real + M_self applied to all 16 right-hand sides in one
+48-component mesh pass.  Inputs are seeded synthetic data (the reference
+ships no dataset).  Every timed step reads and writes buffers far larger
+than the 129 MB L2 (the FP32 mesh alone is 3.2 GB), so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU path for the same workload on
+the host cores (the reference compiled from its sources where available,
+else the oracle's C restatement of it) and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RPY M·f applies/s/RHS (ns/particle), FP32-batched vs FP64, rel-L2 ≤1e-5"
+UNIT = "ns/particle/RHS"
+
+WORKLOADS = {
+    "large": dict(N=1_000_000, L=480.0, K=256, p=6, R=16, xi=0.3, rc=10.0, a=1.0),
+    "multi_rhs": dict(N=200_000, L=250.0, K=160, p=6, R=16, xi=0.3, rc=10.0, a=1.0),
+    "scale_up": dict(N=100_000, L=220.0, K=128, p=6, R=1, xi=0.3, rc=10.0, a=1.0),
+}
+
+# DRAM bytes per launch measured with ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) for the large workload; None until captured.
+NCU_TRAFFIC = {}
+
+
+def algorithmic_bytes(w, s=4):
+    """Bytes each kernel must move at minimum (per launch)."""
+    K, N, C = w["K"], w["N"], 3 * w["R"]
+    Kr, Kc = K ** 3, K * K * (K // 2 + 1)
+    return {
+        "spread": C * s * Kr,                      # mesh written once
+        "influence": C * 4 * s * Kc + s * Kc,      # complex mesh read+write, table once
+        "interp": C * s * Kr + s * C * N,          # mesh read once, result written
+    }
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def synth(w, seed):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0.0, w["L"], size=(w["N"], 3))
+    f = rng.standard_normal((w["R"], 3 * w["N"])).astype(np.float32)
+    return pos, f
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_oracle_time(w, reps_min=1, budget_s=20.0):
+    """The oracle (C restatement of the reference path + Beenakker real/self),
+    FP64, all host cores, one right-hand side of the full system per rep."""
+    import oracle
+    oracle.build()
+    pos, f = synth(w, seed=99)
+    f1 = f[:1].astype(np.float64)
+    nth = os.cpu_count() or 1
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < reps_min or (time.perf_counter() - t_start < budget_s and len(times) < 3):
+        t0 = time.perf_counter()
+        oracle.full(pos, w["L"], w["xi"], w["rc"], w["K"], w["p"], f1, radius=w["a"],
+                    nthreads=nth)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    t0 = time.perf_counter()
+    oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f1, radius=w["a"], nthreads=nth)
+    t_recip = time.perf_counter() - t0
+    ns = t * 1e9 / w["N"]
+    return {"value": ns, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"1 right-hand side of the full N={w['N']} system per rep, best of "
+                      f"{len(times)}; FP64 oracle (reference recip path restated + real-space/self)",
+            "recip_only_value": t_recip * 1e9 / w["N"]}
+
+
+def run_reference(args, w):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    base = cpu_oracle_time(w, reps_min=1, budget_s=0.0)  # warm the build and caches
+    times = []
+    import oracle
+    pos, f = synth(w, seed=7)
+    f1 = f[:1].astype(np.float64)
+    nth = os.cpu_count() or 1
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle.full(pos, w["L"], w["xi"], w["rc"], w["K"], w["p"], f1, radius=w["a"],
+                    nthreads=nth)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    ms = 1e3 * statistics.mean(times)
+    value = ms * 1e6 / w["N"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: positions U[0,L), forces N(0,1), seeded",
+        "config": config_of(w, args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                         "sample": "each step: 1 right-hand side of the full system, FP64 "
+                                   "oracle restatement of the reference CPU path "
+                                   "(compiled reference unavailable on this host)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "recip_only_ns": base["recip_only_value"],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_of(w, args):
+    return {"workload": f"uniform spheres N={w['N']}, L={w['L']}, K={w['K']}, p={w['p']}, "
+                        f"R={w['R']}, xi={w['xi']}, rc={w['rc']}, a={w['a']}",
+            "N": w["N"], "L": w["L"], "K": w["K"], "p": w["p"], "R": w["R"], "xi": w["xi"],
+            "rc": w["rc"], "radius": w["a"], "terms": "recip+real+self",
+            "l2": "inputs larger than L2 (FP32 mesh 3.2 GB per pass); no flush",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
+def run_gb300(args, w):
+    import torch
+
+    import spme_gb300
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    cpu_base = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu_base = cpu_oracle_time(w)  # before any GPU work in this process
+
+    N, R = w["N"], w["R"]
+    pos, f = synth(w, seed=1000 + rank)
+    stream = torch.cuda.current_stream()
+    eng = spme_gb300.Engine(N, w["L"], w["xi"], w["K"], w["p"], radius=w["a"], rcut=w["rc"],
+                            precision="fp32", max_nrhs=R, terms=spme_gb300.TERM_ALL)
+    eng.set_stream(stream.cuda_stream)
+    pos_d = torch.tensor(pos, device="cuda")
+    f_d = torch.tensor(f, device="cuda")
+    u_d = torch.zeros_like(f_d)
+
+    def step():
+        eng.set_positions(pos_d)
+        eng.apply(f_d, u_d)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    eng.set_profiling(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = eng.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = eng.launch_count() - l0
+    ck = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    stages = eng.stage_times()
+    eng.set_profiling(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = ms * 1e6 / (N * R)  # per-rank work fixed (weak scaling): time per unit on each
+
+    # end to end through the public API with pinned host buffers
+    pos_h = torch.tensor(pos).pin_memory().numpy()
+    f_h = torch.tensor(f).pin_memory().numpy()
+    u_h = torch.zeros(f.shape, dtype=torch.float32).pin_memory().numpy()
+    eng.set_stream(None)
+    for _ in range(max(1, args.warmup)):
+        eng.set_positions(pos_h)
+        eng.apply(f_h, u_h)
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        eng.set_positions(pos_h)
+        eng.apply(f_h, u_h)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.mean(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # FP64 plain single-RHS path and accuracy of the FP32 batch against it
+    extra = {}
+    if rank == 0 and not args.no_fp64:
+        e64 = spme_gb300.Engine(N, w["L"], w["xi"], w["K"], w["p"], radius=w["a"],
+                                rcut=w["rc"], precision="fp64", max_nrhs=1,
+                                terms=spme_gb300.TERM_ALL)
+        e64.set_stream(stream.cuda_stream)
+        p64 = torch.tensor(pos, device="cuda")
+        f64 = torch.tensor(f[:1].astype(np.float64), device="cuda")
+        u64 = torch.zeros_like(f64)
+        e64.set_positions(p64)
+        e64.apply(f64, u64)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 3
+        a0.record(stream)
+        for _ in range(reps):
+            e64.set_positions(p64)
+            e64.apply(f64, u64)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = a0.elapsed_time(a1) / reps
+        ref = u64[0].double()
+        got = u_d[0].double()
+        rel = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        ns64 = ms64 * 1e6 / N
+        kmax = np.pi * w["K"] / w["L"]
+        extra = {"fp64_plain": {"value": ns64, "unit": UNIT, "ms_per_apply": ms64,
+                                "terms": "recip+real+self", "nrhs": 1},
+                 "fp32_batched_speedup_vs_fp64_plain": ns64 / value,
+                 "accuracy": {"rel_l2_fp32_vs_fp64": rel,
+                              "spme_truncation_recip": float(np.exp(-kmax ** 2 / (4 * w["xi"] ** 2))),
+                              "spme_truncation_real": float(np.exp(-(w["xi"] * w["rc"]) ** 2))}}
+        e64.close()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(w)
+    kern = {}
+    for k in ("spread", "influence", "interp"):
+        t_ms = stages.get(k, 0.0)
+        if t_ms > 0:
+            gbs = alg[k] / (t_ms * 1e-3) / 1e9
+            kern[k] = {"ms": t_ms, "alg_bytes": alg[k], "achieved_gbs": gbs,
+                       "frac": gbs / peak}
+    for k in ("pack", "realspace", "fft_fwd", "fft_bwd", "unpack"):
+        if k in stages:
+            kern[k] = {"ms": stages[k]}
+    dom = max(("spread", "influence", "interp"), key=lambda k: kern.get(k, {}).get("ms", 0.0))
+    roof = None
+    if dom in kern:
+        tr = NCU_TRAFFIC.get(dom)
+        roof = {"kernel": dom, "bound": "hbm", "achieved": kern[dom]["achieved_gbs"],
+                "peak": peak, "unit": "GB/s", "frac": kern[dom]["achieved_gbs"] / peak,
+                "traffic": tr, "peak_kind": peak_kind}
+    h2d = pos.nbytes + f.nbytes
+    d2h = f.nbytes
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: positions U[0,L) and forces N(0,1), seeded",
+        "config": config_of(w, args),
+        "roofline": roof,
+        "cpu_baseline": cpu_base,
+        "e2e": {"value": e2e_ms * 1e6 / (N * R), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "clocks": ck,
+        "gpu_launches": launches,
+        "kernels": kern,
+    }
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_gb300(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,120 @@
+/*
+ * spme_gb300.h — extended C ABI of the GB300 SPME-RPY mobility operator.
+ *
+ * The reference (billy-inn/SPME) has only the spme.h entry points
+ * (old-version/spme.h:85-97) and computes only the reciprocal-space part with
+ * radius 1.  These entry points add what the reference's callers (block
+ * Krylov / Lanczos Brownian-dynamics samplers) need around that apply:
+ *   - the full Ewald-split RPY mobility  M = M_recip + M_real + M_self
+ *     for any radius a and real-space cutoff rc (Beenakker 1986 splitting);
+ *   - FP32 batching of R right-hand sides through one mesh pass (3R
+ *     components), with FP64 kept for fractional coordinates, the moduli and
+ *     influence tables, and the real-space / self accumulation;
+ *   - host or device-resident vectors, and a caller-chosen CUDA stream;
+ *   - integer status codes instead of the reference's asserts.
+ *
+ * Units follow the reference's scalar_recip (old-version/spme.c:43-60): the
+ * mobility times 6*pi*eta, so an isolated sphere of radius a has
+ * self-mobility 1/a.
+ *
+ * Vector layout everywhere is compute_spme's (old-version/spme.h:95-97):
+ * right-hand side r of particle i, Cartesian d, at v[r*ld + 3*i + d].
+ * Element type is double for SPME_FP64 engines and float for SPME_FP32.
+ *
+ * An engine is bound to the device that was current at spme_create.  It is
+ * not thread-safe; separate engines may be used from separate threads.
+ */
+#ifndef SPME_GB300_EXT_H
+#define SPME_GB300_EXT_H
+
+#include "spme.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+    SPME_OK = 0,
+    SPME_ERR_INVALID = 1,     /* bad argument */
+    SPME_ERR_UNSUPPORTED = 2, /* valid but outside what this build supports */
+    SPME_ERR_CUDA = 3,        /* CUDA runtime error */
+    SPME_ERR_CUFFT = 4,       /* cuFFT error */
+    SPME_ERR_NOMEM = 5,       /* device or host allocation failed */
+    SPME_ERR_STATE = 6,       /* e.g. apply before any positions were given */
+    SPME_ERR_KERNEL = 7       /* a device-side check failed (status read back) */
+};
+
+enum { SPME_FP64 = 0, SPME_FP32 = 1 };
+
+enum {
+    SPME_TERM_RECIP = 1,
+    SPME_TERM_REAL = 2,
+    SPME_TERM_SELF = 4,
+    SPME_TERM_ALL = 7
+};
+
+enum { SPME_MEM_HOST = 0, SPME_MEM_DEVICE = 1 };
+
+typedef struct spme_params {
+    int np;           /* particles, >= 0 */
+    int dim;          /* mesh size K per axis, 2..1024 */
+    int porder;       /* B-spline order p: 4, 6 or 8 */
+    double box_size;  /* cubic periodic box edge L > 0 */
+    double xi;        /* Ewald splitting parameter > 0 */
+    double radius;    /* particle radius a > 0 (the reference fixes 1) */
+    double rcut;      /* real-space cutoff, 0 < rc < L/2 (needed if SPME_TERM_REAL) */
+    int precision;    /* SPME_FP64 or SPME_FP32 */
+    int max_nrhs;     /* right-hand sides carried per mesh pass, >= 1 */
+    int terms;        /* OR of SPME_TERM_* */
+} spme_params;
+
+/* Fill *p with defaults: radius 1, precision FP64, max_nrhs 1, terms RECIP
+ * (the reference's operator); np/dim/porder/box_size/xi/rcut zero. */
+void spme_params_init(spme_params *p);
+
+/* Create an engine (allocates device memory, cuFFT plans, tables). */
+int spme_create(const spme_params *params, spme_t **out);
+
+/* Destroy an engine; NULL is a no-op. */
+int spme_destroy(spme_t *spme);
+
+/* Run subsequent work on `stream` (a cudaStream_t; NULL = the engine's own). */
+int spme_set_stream(spme_t *spme, void *stream);
+
+/* Load positions (np x 3 doubles; host or device per `mem`) and build the
+ * B-spline records, the mesh-tile sort and the real-space cell list.
+ * Positions outside [0, L) are wrapped. */
+int spme_set_positions(spme_t *spme, const double *pos, int mem);
+
+/* u_r = beta*u_r + alpha * M f_r for r < nrhs (any nrhs >= 0; passes of at
+ * most max_nrhs).  f and u are host or device pointers per `mem`, element
+ * type per the engine's precision, layout v[r*ld + 3*i + d], ld >= 3*np.
+ * Host calls return after the result is in u; device calls are
+ * stream-ordered on the engine's stream. */
+int spme_apply(spme_t *spme, int nrhs, double alpha, const void *f, long ldf, double beta,
+               void *u, long ldu, int mem);
+
+/* Block until the engine's stream is idle. */
+int spme_synchronize(spme_t *spme);
+
+/* Per-stage device times (ms) of the last apply when profiling is on
+ * (spme_set_profiling(spme, 1)).  Stages, in order: pack, real-space,
+ * spread, forward FFT, influence, backward FFT, interpolate, unpack.
+ * Returns the number of stages written (<= n). */
+int spme_set_profiling(spme_t *spme, int on);
+int spme_stage_times(const spme_t *spme, float *ms, int n);
+
+/* Number of kernels this engine launched since creation (cuFFT launches
+ * counted as the plan's kernels are not visible here: one per FFT call). */
+long spme_launch_count(const spme_t *spme);
+
+/* Mesh-tile shape used by spread/interpolate (default 8 x 8 x 8; each 1..16).
+ * Takes effect at the next spme_set_positions. */
+int spme_set_tile(spme_t *spme, int tx, int ty, int tz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPME_GB300_EXT_H */

@@ -1,0 +1,659 @@
+// Host engine and C ABI of the GB300 SPME-RPY mobility operator.
+//
+// Orchestrates, per mesh pass of R right-hand sides (C = 3R components):
+//   pack -> [aux stream: real-space + self] -> spread -> cuFFT R2C ->
+//   influence -> cuFFT C2R -> interpolate (+ real-space result) -> unpack
+// The reference's compute_spme (old-version/spme.c:560-726) runs the whole
+// pipeline once per right-hand side; here one pass carries up to max_nrhs.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "kernels.h"
+#include "spme_gb300.h"
+
+using spme::MeshGeom;
+
+namespace {
+
+constexpr int kStages = 8;
+
+struct PlanPair {
+    int C;
+    cufftHandle fwd;
+    cufftHandle bwd;
+};
+
+}  // namespace
+
+struct _spme_t {
+    spme_params prm;
+    int device = 0;
+    int last_error = SPME_OK;
+    cudaStream_t own_stream = nullptr, stream = nullptr, aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool profiling = false;
+    cudaEvent_t ev[kStages + 1] = {};
+    cudaEvent_t ev_rs[2] = {};
+    float stage_ms[kStages] = {};
+    bool stages_valid = false;
+    bool ran_real = false;
+    long launches = 0;
+    MeshGeom g{};
+    int tile[3] = {8, 8, 8};
+    size_t elem = 8;
+    int Cmax = 3;
+    int ntiles = 0;
+    int nc = 1;
+    bool have_pos = false;
+    // device buffers
+    double *d_pos = nullptr;
+    int *d_key = nullptr, *d_slot = nullptr, *d_tcount = nullptr, *d_toff = nullptr,
+        *d_tperm = nullptr, *d_scan_tmp = nullptr;
+    int *d_rec_idx = nullptr;
+    uint32_t *d_rec_start = nullptr;
+    void *d_rec_w = nullptr;
+    int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
+    double4 *d_cpos = nullptr;
+    void *d_mesh = nullptr, *d_cmesh = nullptr, *d_tab = nullptr;
+    double *d_bmod2 = nullptr;
+    void *d_work = nullptr;
+    size_t work_bytes = 0;
+    std::vector<PlanPair> plans;
+    void *d_F = nullptr, *d_W = nullptr, *d_fstage = nullptr, *d_ustage = nullptr;
+    size_t cap_tiles = 0;  // allocated tile-count capacity
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+        else prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+int from_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return SPME_OK;
+    if (e == cudaErrorMemoryAllocation) return SPME_ERR_NOMEM;
+    return SPME_ERR_CUDA;
+}
+
+int from_cufft(cufftResult r) {
+    if (r == CUFFT_SUCCESS) return SPME_OK;
+    if (r == CUFFT_ALLOC_FAILED) return SPME_ERR_NOMEM;
+    return SPME_ERR_CUFFT;
+}
+
+#define TRY_CUDA(x)                              \
+    do {                                         \
+        cudaError_t e_ = (x);                    \
+        if (e_ != cudaSuccess) return from_cuda(e_); \
+    } while (0)
+#define TRY_FFT(x)                               \
+    do {                                         \
+        cufftResult r_ = (x);                    \
+        if (r_ != CUFFT_SUCCESS) return from_cufft(r_); \
+    } while (0)
+#define TRY(x)                                   \
+    do {                                         \
+        int s_ = (x);                            \
+        if (s_ != SPME_OK) return s_;            \
+    } while (0)
+
+template <typename P>
+int dalloc(P **p, size_t bytes) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes < 256 ? 256 : bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return SPME_ERR_NOMEM;
+    }
+    *p = reinterpret_cast<P *>(q);
+    return SPME_OK;
+}
+
+void dfree(void *p) {
+    if (p) cudaFree(p);
+}
+
+// Host B-spline values M_p(w + p - 1 - j) (same recursion as the kernels).
+void host_bspline(int p, double w, double *out) {
+    double a[spme::kMaxP + 1];
+    a[0] = w;
+    a[1] = 1.0 - w;
+    for (int n = 3; n <= p; n++) {
+        a[n - 1] = 0.0;
+        for (int k = n - 1; k >= 1; k--)
+            a[k] = ((w + k) * a[k] + ((double)n - w - k) * a[k - 1]) / (double)(n - 1);
+        a[0] = w * a[0] / (double)(n - 1);
+    }
+    for (int k = 0; k < p; k++) out[k] = a[p - 1 - k];
+}
+
+// |b(m)|^2 = 1/|sum_{j<p-1} M_p(j+1) e^{i j phi}|^2, phi = 2 pi m'/K
+// (old-version/spme.c:109-126; only the modulus enters the table).
+void host_moduli2(int K, int p, std::vector<double> &out) {
+    double mp[spme::kMaxP];
+    host_bspline(p, 0.0, mp);  // mp[j] = M_p(p - 1 - j)
+    out.resize(K);
+    for (int m = 0; m < K; m++) {
+        int mm = m <= K / 2 ? m : m - K;
+        double phi = 2.0 * M_PI * (double)mm / (double)K;
+        double re = 0.0, im = 0.0;
+        for (int j = 0; j < p - 1; j++) {
+            double s = mp[p - 2 - j];
+            re += s * std::cos(j * phi);
+            im += s * std::sin(j * phi);
+        }
+        out[m] = 1.0 / (re * re + im * im);
+    }
+}
+
+bool is_fp32(const spme_t *e) { return e->prm.precision == SPME_FP32; }
+
+// Beenakker's self term in mobility x 6 pi eta units: (1 - 6 xi a/sqrt(pi)
+// + 40 xi^3 a^3 / (3 sqrt(pi))) / a.
+double self_coeff(double xi, double a) {
+    const double rsp = 0.56418958354775628695;
+    return (1.0 - 6.0 * xi * a * rsp + 40.0 / 3.0 * xi * xi * xi * a * a * a * rsp) / a;
+}
+
+int validate(const spme_params &p) {
+    if (p.np < 0 || p.dim < 2 || p.dim > 1024) return SPME_ERR_INVALID;
+    if (p.porder != 4 && p.porder != 6 && p.porder != 8) return SPME_ERR_UNSUPPORTED;
+    if (p.dim < p.porder) return SPME_ERR_UNSUPPORTED;
+    if (!(p.box_size > 0.0) || !(p.xi > 0.0) || !(p.radius > 0.0)) return SPME_ERR_INVALID;
+    if (p.precision != SPME_FP64 && p.precision != SPME_FP32) return SPME_ERR_INVALID;
+    if (p.max_nrhs < 1 || p.max_nrhs > 1024) return SPME_ERR_INVALID;
+    if (p.terms <= 0 || (p.terms & ~SPME_TERM_ALL)) return SPME_ERR_INVALID;
+    if ((p.terms & SPME_TERM_REAL) && !(p.rcut > 0.0 && p.rcut < 0.5 * p.box_size))
+        return SPME_ERR_INVALID;
+    return SPME_OK;
+}
+
+void set_geometry(spme_t *e) {
+    MeshGeom &g = e->g;
+    g.K = e->prm.dim;
+    g.p = e->prm.porder;
+    g.L = e->prm.box_size;
+    g.tx = std::min(e->tile[0], g.K);
+    g.ty = std::min(e->tile[1], g.K);
+    g.tz = std::min(e->tile[2], g.K);
+    g.ntx = (g.K + g.tx - 1) / g.tx;
+    g.nty = (g.K + g.ty - 1) / g.ty;
+    g.ntz = (g.K + g.tz - 1) / g.tz;
+    e->ntiles = g.ntx * g.nty * g.ntz;
+}
+
+int record_width(const spme_t *e) {
+    int raw = 3 * e->prm.porder, per16 = (int)(16 / e->elem);
+    return (raw + per16 - 1) / per16 * per16;
+}
+
+int alloc_tiles(spme_t *e) {
+    size_t need = (size_t)e->ntiles;
+    if (need <= e->cap_tiles && e->d_tcount) return SPME_OK;
+    dfree(e->d_tcount);
+    dfree(e->d_toff);
+    dfree(e->d_scan_tmp);
+    e->d_tcount = e->d_toff = e->d_scan_tmp = nullptr;
+    size_t ncell = (size_t)e->nc * e->nc * e->nc;
+    size_t nkeys = std::max(need, ncell);
+    TRY(dalloc(&e->d_tcount, sizeof(int) * need));
+    TRY(dalloc(&e->d_toff, sizeof(int) * (need + 1)));
+    TRY(dalloc(&e->d_scan_tmp, sizeof(int) * spme::scan_tmp_elems((int)nkeys)));
+    e->cap_tiles = need;
+    return SPME_OK;
+}
+
+int get_plans(spme_t *e, int C, PlanPair **out) {
+    for (PlanPair &p : e->plans)
+        if (p.C == C) {
+            *out = &p;
+            return SPME_OK;
+        }
+    const int K = e->prm.dim;
+    int n[3] = {K, K, K}, re[3] = {K, K, K}, ce[3] = {K, K, K / 2 + 1};
+    PlanPair pp;
+    pp.C = C;
+    size_t ws1 = 0, ws2 = 0;
+    TRY_FFT(cufftCreate(&pp.fwd));
+    TRY_FFT(cufftCreate(&pp.bwd));
+    TRY_FFT(cufftSetAutoAllocation(pp.fwd, 0));
+    TRY_FFT(cufftSetAutoAllocation(pp.bwd, 0));
+    cufftType tf = is_fp32(e) ? CUFFT_R2C : CUFFT_D2Z;
+    cufftType tb = is_fp32(e) ? CUFFT_C2R : CUFFT_Z2D;
+    TRY_FFT(cufftMakePlanMany(pp.fwd, 3, n, re, C, 1, ce, C, 1, tf, C, &ws1));
+    TRY_FFT(cufftMakePlanMany(pp.bwd, 3, n, ce, C, 1, re, C, 1, tb, C, &ws2));
+    size_t ws = std::max(ws1, ws2);
+    if (ws > e->work_bytes) {
+        dfree(e->d_work);
+        e->d_work = nullptr;
+        e->work_bytes = 0;
+        TRY(dalloc(&e->d_work, ws));
+        e->work_bytes = ws;
+        for (PlanPair &q : e->plans) {
+            TRY_FFT(cufftSetWorkArea(q.fwd, e->d_work));
+            TRY_FFT(cufftSetWorkArea(q.bwd, e->d_work));
+        }
+    }
+    TRY_FFT(cufftSetWorkArea(pp.fwd, e->d_work));
+    TRY_FFT(cufftSetWorkArea(pp.bwd, e->d_work));
+    TRY_FFT(cufftSetStream(pp.fwd, e->stream));
+    TRY_FFT(cufftSetStream(pp.bwd, e->stream));
+    e->plans.push_back(pp);
+    *out = &e->plans.back();
+    return SPME_OK;
+}
+
+int create_impl(const spme_params &prm, spme_t **out) {
+    TRY(validate(prm));
+    spme_t *e = new (std::nothrow) _spme_t();
+    if (!e) return SPME_ERR_NOMEM;
+    *out = e;
+    e->prm = prm;
+    cudaGetDevice(&e->device);
+    e->elem = is_fp32(e) ? sizeof(float) : sizeof(double);
+    e->Cmax = 3 * prm.max_nrhs;
+    set_geometry(e);
+    if (prm.terms & SPME_TERM_REAL) {
+        long nc = (long)std::floor(prm.box_size / prm.rcut);
+        long cap = std::max<long>(3, (long)std::cbrt(8.0 * prm.np + 27.0));
+        nc = std::min(nc, std::min(cap, 1024L));
+        e->nc = nc < 3 ? 1 : (int)nc;
+    }
+    TRY_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
+    TRY_CUDA(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking));
+    e->stream = e->own_stream;
+    TRY_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+    TRY_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+    for (int i = 0; i <= kStages; i++) TRY_CUDA(cudaEventCreate(&e->ev[i]));
+    TRY_CUDA(cudaEventCreate(&e->ev_rs[0]));
+    TRY_CUDA(cudaEventCreate(&e->ev_rs[1]));
+
+    const size_t n = (size_t)prm.np, K = (size_t)prm.dim, Kh = K / 2 + 1;
+    const size_t C = (size_t)e->Cmax;
+    TRY(dalloc(&e->d_pos, sizeof(double) * 3 * n));
+    TRY(dalloc(&e->d_key, sizeof(int) * n));
+    TRY(dalloc(&e->d_slot, sizeof(int) * n));
+    TRY(dalloc(&e->d_tperm, sizeof(int) * n));
+    TRY(alloc_tiles(e));
+    TRY(dalloc(&e->d_rec_idx, sizeof(int) * n));
+    TRY(dalloc(&e->d_rec_start, sizeof(uint32_t) * n));
+    TRY(dalloc(&e->d_rec_w, e->elem * record_width(e) * n));
+    if (prm.terms & SPME_TERM_REAL) {
+        size_t ncell = (size_t)e->nc * e->nc * e->nc;
+        TRY(dalloc(&e->d_ccount, sizeof(int) * ncell));
+        TRY(dalloc(&e->d_coff, sizeof(int) * (ncell + 1)));
+        TRY(dalloc(&e->d_cperm, sizeof(int) * n));
+        TRY(dalloc(&e->d_cpos, sizeof(double4) * n));
+    }
+    if (prm.terms & SPME_TERM_RECIP) {
+        TRY(dalloc(&e->d_mesh, e->elem * K * K * K * C));
+        TRY(dalloc(&e->d_cmesh, 2 * e->elem * K * K * Kh * C));
+        TRY(dalloc(&e->d_tab, 2 * e->elem * K * K * Kh));
+        TRY(dalloc(&e->d_bmod2, sizeof(double) * K));
+        std::vector<double> bm;
+        host_moduli2((int)K, prm.porder, bm);
+        TRY_CUDA(cudaMemcpyAsync(e->d_bmod2, bm.data(), sizeof(double) * K,
+                                 cudaMemcpyHostToDevice, e->stream));
+        if (is_fp32(e))
+            spme::launch_influence_table<float>((float *)e->d_tab, e->d_bmod2, (int)K,
+                                                prm.box_size, prm.xi, prm.radius, e->stream);
+        else
+            spme::launch_influence_table<double>((double *)e->d_tab, e->d_bmod2, (int)K,
+                                                 prm.box_size, prm.xi, prm.radius, e->stream);
+        e->launches++;
+        TRY_CUDA(cudaGetLastError());
+        PlanPair *pp;
+        TRY(get_plans(e, (int)C, &pp));
+    }
+    TRY(dalloc(&e->d_F, e->elem * n * C));
+    TRY(dalloc(&e->d_W, e->elem * n * C));
+    TRY(dalloc(&e->d_fstage, e->elem * n * C));
+    TRY(dalloc(&e->d_ustage, e->elem * n * C));
+    TRY_CUDA(cudaStreamSynchronize(e->stream));
+    return SPME_OK;
+}
+
+void destroy_impl(spme_t *e) {
+    if (!e) return;
+    DeviceGuard dg(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->aux) cudaStreamSynchronize(e->aux);
+    for (PlanPair &p : e->plans) {
+        cufftDestroy(p.fwd);
+        cufftDestroy(p.bwd);
+    }
+    void *bufs[] = {e->d_pos,    e->d_key,     e->d_slot,  e->d_tcount,   e->d_toff,
+                    e->d_tperm,  e->d_scan_tmp, e->d_rec_idx, e->d_rec_start, e->d_rec_w,
+                    e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_mesh,
+                    e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
+                    e->d_W,      e->d_fstage,  e->d_ustage};
+    for (void *b : bufs) dfree(b);
+    for (int i = 0; i <= kStages; i++)
+        if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+    if (e->ev_rs[0]) cudaEventDestroy(e->ev_rs[0]);
+    if (e->ev_rs[1]) cudaEventDestroy(e->ev_rs[1]);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
+    if (e->aux) cudaStreamDestroy(e->aux);
+    if (e->own_stream) cudaStreamDestroy(e->own_stream);
+    delete e;
+}
+
+int set_positions_impl(spme_t *e, const double *pos, int mem) {
+    const int n = e->prm.np;
+    cudaStream_t s = e->stream;
+    if (n > 0) {
+        if (!pos) return SPME_ERR_INVALID;
+        TRY_CUDA(cudaMemcpyAsync(e->d_pos, pos, sizeof(double) * 3 * n,
+                                 mem == SPME_MEM_HOST ? cudaMemcpyHostToDevice
+                                                      : cudaMemcpyDeviceToDevice,
+                                 s));
+    }
+    if (e->prm.terms & SPME_TERM_RECIP) {
+        set_geometry(e);
+        TRY(alloc_tiles(e));
+        TRY_CUDA(cudaMemsetAsync(e->d_tcount, 0, sizeof(int) * e->ntiles, s));
+        spme::launch_tile_keys(e->d_pos, n, e->g, e->d_key, e->d_tcount, e->d_slot, s);
+        spme::launch_scan(e->d_tcount, e->ntiles, e->d_toff, e->d_scan_tmp, s);
+        spme::launch_scatter(e->d_key, e->d_slot, e->d_toff, n, e->d_tperm, s);
+        if (is_fp32(e))
+            spme::launch_records<float>(e->d_pos, e->d_tperm, n, e->g, e->d_rec_idx,
+                                        e->d_rec_start, (float *)e->d_rec_w, s);
+        else
+            spme::launch_records<double>(e->d_pos, e->d_tperm, n, e->g, e->d_rec_idx,
+                                         e->d_rec_start, (double *)e->d_rec_w, s);
+        e->launches += 6;
+    }
+    if (e->prm.terms & SPME_TERM_REAL) {
+        int ncell = e->nc * e->nc * e->nc;
+        TRY_CUDA(cudaMemsetAsync(e->d_ccount, 0, sizeof(int) * ncell, s));
+        spme::launch_cell_keys(e->d_pos, n, e->prm.box_size, e->nc, e->d_key, e->d_ccount,
+                               e->d_slot, s);
+        spme::launch_scan(e->d_ccount, ncell, e->d_coff, e->d_scan_tmp, s);
+        spme::launch_scatter(e->d_key, e->d_slot, e->d_coff, n, e->d_cperm, s);
+        spme::launch_cell_positions(e->d_pos, e->d_cperm, n, e->prm.box_size, e->d_cpos, s);
+        e->launches += 6;
+    }
+    TRY_CUDA(cudaGetLastError());
+    e->have_pos = true;
+    return SPME_OK;
+}
+
+template <typename T>
+int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alpha, double beta) {
+    const int n = e->prm.np, C = 3 * R, K = e->prm.dim;
+    const int terms = e->prm.terms;
+    cudaStream_t s = e->stream;
+    const bool rs = (terms & (SPME_TERM_REAL | SPME_TERM_SELF)) != 0;
+    const bool prof = e->profiling;
+    T *F = (T *)e->d_F, *W = (T *)e->d_W;
+    if (prof) cudaEventRecord(e->ev[0], s);
+    spme::launch_pack<T>(f, ldf, n, R, F, s);
+    e->launches++;
+    if (prof) cudaEventRecord(e->ev[1], s);
+    if (rs) {
+        TRY_CUDA(cudaEventRecord(e->ev_fork, s));
+        TRY_CUDA(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
+        if (prof) cudaEventRecord(e->ev_rs[0], e->aux);
+        if (terms & SPME_TERM_REAL) {
+            if (!e->d_coff || !e->d_cperm || !e->d_cpos) return SPME_ERR_STATE;
+            TRY_CUDA(spme::launch_realspace<T>(e->nc, e->d_coff, e->d_cperm, e->d_cpos, F, R,
+                                               e->prm.box_size, e->prm.rcut, e->prm.xi,
+                                               e->prm.radius, 1,
+                                               (terms & SPME_TERM_SELF) ? 1 : 0, W, e->aux));
+        } else {
+            spme::launch_self<T>(F, n, R, self_coeff(e->prm.xi, e->prm.radius), W, e->aux);
+        }
+        e->launches++;
+        if (prof) cudaEventRecord(e->ev_rs[1], e->aux);
+        TRY_CUDA(cudaEventRecord(e->ev_join, e->aux));
+    }
+    if (terms & SPME_TERM_RECIP) {
+        if (!e->d_mesh || !e->d_cmesh || !e->d_tab) return SPME_ERR_STATE;
+        PlanPair *pp;
+        TRY(get_plans(e, C, &pp));
+        TRY_CUDA(spme::launch_spread<T>(e->d_toff, e->d_rec_idx, e->d_rec_start,
+                                        (const T *)e->d_rec_w, F, C, e->g, (T *)e->d_mesh, s));
+        e->launches++;
+        if (prof) cudaEventRecord(e->ev[2], s);
+        if (sizeof(T) == 4)
+            TRY_FFT(cufftExecR2C(pp->fwd, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh));
+        else
+            TRY_FFT(cufftExecD2Z(pp->fwd, (cufftDoubleReal *)e->d_mesh,
+                                 (cufftDoubleComplex *)e->d_cmesh));
+        if (prof) cudaEventRecord(e->ev[3], s);
+        spme::launch_influence<T>((T *)e->d_cmesh, (const T *)e->d_tab, K, e->prm.box_size, R, s);
+        e->launches += 2;
+        if (prof) cudaEventRecord(e->ev[4], s);
+        if (sizeof(T) == 4)
+            TRY_FFT(cufftExecC2R(pp->bwd, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh));
+        else
+            TRY_FFT(cufftExecZ2D(pp->bwd, (cufftDoubleComplex *)e->d_cmesh,
+                                 (cufftDoubleReal *)e->d_mesh));
+        if (prof) cudaEventRecord(e->ev[5], s);
+        if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
+        TRY_CUDA(spme::launch_interp<T>(n, e->d_rec_idx, e->d_rec_start, (const T *)e->d_rec_w,
+                                        (const T *)e->d_mesh, C, e->g, W, rs ? 1 : 0, s));
+        e->launches++;
+        if (prof) cudaEventRecord(e->ev[6], s);
+    } else {
+        TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
+        if (prof)
+            for (int k = 2; k <= 6; k++) cudaEventRecord(e->ev[k], s);
+    }
+    spme::launch_unpack<T>(W, n, R, alpha, beta, u, ldu, s);
+    e->launches++;
+    if (prof) cudaEventRecord(e->ev[7], s);
+    e->ran_real = rs;
+    e->stages_valid = prof;
+    return from_cuda(cudaGetLastError());
+}
+
+int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, double beta, void *u,
+               long ldu, int mem) {
+    const int n = e->prm.np;
+    if (nrhs < 0 || (mem != SPME_MEM_HOST && mem != SPME_MEM_DEVICE)) return SPME_ERR_INVALID;
+    if (nrhs == 0 || n == 0) return SPME_OK;
+    if (!f || !u || ldf < 3L * n || ldu < 3L * n) return SPME_ERR_INVALID;
+    if (!e->have_pos) return SPME_ERR_STATE;
+    const size_t el = e->elem, row = el * 3 * (size_t)n;
+    for (int r0 = 0; r0 < nrhs; r0 += e->prm.max_nrhs) {
+        const int R = std::min(e->prm.max_nrhs, nrhs - r0);
+        const char *fp = (const char *)f + el * (size_t)r0 * ldf;
+        char *up = (char *)u + el * (size_t)r0 * ldu;
+        int st;
+        if (mem == SPME_MEM_HOST) {
+            TRY_CUDA(cudaMemcpy2DAsync(e->d_fstage, row, fp, el * ldf, row, R,
+                                       cudaMemcpyHostToDevice, e->stream));
+            if (beta != 0.0)
+                TRY_CUDA(cudaMemcpy2DAsync(e->d_ustage, row, up, el * ldu, row, R,
+                                           cudaMemcpyHostToDevice, e->stream));
+            if (is_fp32(e))
+                st = run_pass<float>(e, R, (const float *)e->d_fstage, 3L * n,
+                                     (float *)e->d_ustage, 3L * n, alpha, beta);
+            else
+                st = run_pass<double>(e, R, (const double *)e->d_fstage, 3L * n,
+                                      (double *)e->d_ustage, 3L * n, alpha, beta);
+            TRY(st);
+            TRY_CUDA(cudaMemcpy2DAsync(up, el * ldu, e->d_ustage, row, row, R,
+                                       cudaMemcpyDeviceToHost, e->stream));
+        } else {
+            if (is_fp32(e))
+                st = run_pass<float>(e, R, (const float *)fp, ldf, (float *)up, ldu, alpha, beta);
+            else
+                st = run_pass<double>(e, R, (const double *)fp, ldf, (double *)up, ldu, alpha,
+                                      beta);
+            TRY(st);
+        }
+    }
+    if (mem == SPME_MEM_HOST) TRY_CUDA(cudaStreamSynchronize(e->stream));
+    return SPME_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void spme_params_init(spme_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->radius = 1.0;
+    p->precision = SPME_FP64;
+    p->max_nrhs = 1;
+    p->terms = SPME_TERM_RECIP;
+}
+
+int spme_create(const spme_params *params, spme_t **out) {
+    if (!params || !out) return SPME_ERR_INVALID;
+    *out = nullptr;
+    spme_t *e = nullptr;
+    int st = create_impl(*params, &e);
+    if (st != SPME_OK) {
+        destroy_impl(e);
+        return st;
+    }
+    *out = e;
+    return SPME_OK;
+}
+
+int spme_destroy(spme_t *e) {
+    destroy_impl(e);
+    return SPME_OK;
+}
+
+int spme_set_stream(spme_t *e, void *stream) {
+    if (!e) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    e->stream = stream ? (cudaStream_t)stream : e->own_stream;
+    for (PlanPair &p : e->plans) {
+        cufftSetStream(p.fwd, e->stream);
+        cufftSetStream(p.bwd, e->stream);
+    }
+    return e->last_error = SPME_OK;
+}
+
+int spme_set_positions(spme_t *e, const double *pos, int mem) {
+    if (!e) return SPME_ERR_INVALID;
+    if (mem != SPME_MEM_HOST && mem != SPME_MEM_DEVICE) return e->last_error = SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    return e->last_error = set_positions_impl(e, pos, mem);
+}
+
+int spme_apply(spme_t *e, int nrhs, double alpha, const void *f, long ldf, double beta, void *u,
+               long ldu, int mem) {
+    if (!e) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    return e->last_error = apply_impl(e, nrhs, alpha, f, ldf, beta, u, ldu, mem);
+}
+
+int spme_synchronize(spme_t *e) {
+    if (!e) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    return e->last_error = from_cuda(cudaStreamSynchronize(e->stream));
+}
+
+int spme_set_profiling(spme_t *e, int on) {
+    if (!e) return SPME_ERR_INVALID;
+    e->profiling = on != 0;
+    e->stages_valid = false;
+    return SPME_OK;
+}
+
+int spme_stage_times(const spme_t *e, float *ms, int n) {
+    if (!e || !ms || n < 0 || !e->stages_valid) return 0;
+    DeviceGuard dg(e->device);
+    cudaEventSynchronize(e->ev[kStages - 1]);
+    float t[kStages] = {};
+    cudaEventElapsedTime(&t[0], e->ev[0], e->ev[1]);
+    if (e->ran_real) cudaEventElapsedTime(&t[1], e->ev_rs[0], e->ev_rs[1]);
+    for (int k = 2; k < kStages; k++) {
+        int from = k == 2 ? 1 : k - 1;
+        cudaEventElapsedTime(&t[k], e->ev[from], e->ev[k]);
+    }
+    int m = std::min(n, kStages);
+    for (int k = 0; k < m; k++) ms[k] = t[k];
+    return m;
+}
+
+long spme_launch_count(const spme_t *e) { return e ? e->launches : 0; }
+
+int spme_set_tile(spme_t *e, int tx, int ty, int tz) {
+    if (!e) return SPME_ERR_INVALID;
+    if (tx < 4 || ty < 4 || tz < 4 || tx > spme::kMaxTile || ty > spme::kMaxTile ||
+        tz > spme::kMaxTile)
+        return e->last_error = SPME_ERR_INVALID;
+    e->tile[0] = tx;
+    e->tile[1] = ty;
+    e->tile[2] = tz;
+    e->have_pos = false;
+    return e->last_error = SPME_OK;
+}
+
+int spme_last_error(const spme_t *e) { return e ? e->last_error : SPME_ERR_INVALID; }
+
+const char *spme_error_string(int code) {
+    switch (code) {
+        case SPME_OK: return "success";
+        case SPME_ERR_INVALID: return "invalid argument";
+        case SPME_ERR_UNSUPPORTED: return "unsupported parameters";
+        case SPME_ERR_CUDA: return "CUDA runtime error";
+        case SPME_ERR_CUFFT: return "cuFFT error";
+        case SPME_ERR_NOMEM: return "out of memory";
+        case SPME_ERR_STATE: return "engine state error (positions not set)";
+        case SPME_ERR_KERNEL: return "device-side check failed";
+        default: return "unknown error";
+    }
+}
+
+// ---- drop-in entry points (old-version/spme.h:85-97) ----------------------
+
+void cutoff2xi(double rmax, double ewald_eps, double box_size, double *_xi) {
+    (void)box_size;
+    if (!_xi) return;
+    if (!(rmax > 0.0) || !(ewald_eps > 0.0 && ewald_eps < 1.0)) {
+        *_xi = 0.0;
+        return;
+    }
+    *_xi = std::sqrt(-std::log(ewald_eps)) / rmax;
+}
+
+void create_spme_engine(double xi, int dim, int porder, int np, double box_size, int nthreads,
+                        spme_t **_spme) {
+    (void)nthreads;
+    if (!_spme) return;
+    spme_params p;
+    spme_params_init(&p);
+    p.np = np;
+    p.dim = dim;
+    p.porder = porder;
+    p.box_size = box_size;
+    p.xi = xi;
+    spme_create(&p, _spme);
+}
+
+void destroy_spme_engine(spme_t *spme) { spme_destroy(spme); }
+
+void compute_spme(spme_t *spme, double *pos, int nrhs, double alpha, double *vec_in, int ldin,
+                  double beta, double *vec_out, int ldout) {
+    if (!spme) return;
+    if (pos) {
+        if (spme_set_positions(spme, pos, SPME_MEM_HOST) != SPME_OK) return;
+    }
+    spme_apply(spme, nrhs, alpha, vec_in, ldin, beta, vec_out, ldout, SPME_MEM_HOST);
+}
+
+}  // extern "C"

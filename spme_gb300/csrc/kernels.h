@@ -1,0 +1,81 @@
+// Host-side launchers for the GB300 SPME-RPY kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace spme {
+
+// ---- P-build and counting sorts (pbuild.cu) -------------------------------
+// Tile key of each particle's stencil start, and a slot within its tile.
+void launch_tile_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
+                      int *slot, cudaStream_t s);
+// Real-space cell key (nc^3 cells of edge L/nc) and slot within its cell.
+void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
+                      int *slot, cudaStream_t s);
+// Exclusive scan of count[0..nkeys) into off[0..nkeys] (off[nkeys] = total).
+// tmp must hold scan_tmp_elems(nkeys) ints.
+size_t scan_tmp_elems(int nkeys);
+void launch_scan(const int *count, int nkeys, int *off, int *tmp, cudaStream_t s);
+// perm[off[key[i]] + slot[i]] = i
+void launch_scatter(const int *key, const int *slot, const int *off, int n, int *perm,
+                    cudaStream_t s);
+// B-spline records in tile-sorted order: rec_idx[s] = perm[s], packed stencil
+// start, and p weights per axis (record width RecordWidth<T,P>).
+template <typename T>
+void launch_records(const double *pos, const int *perm, int n, const MeshGeom &g,
+                    int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s);
+// Wrapped positions in cell-sorted order.
+void launch_cell_positions(const double *pos, const int *perm, int n, double L,
+                           double4 *cpos, cudaStream_t s);
+
+// ---- spread / interpolate (spread.cu, interp.cu) --------------------------
+struct CompSplit {
+    int cgp;  // lanes per component group within a warp (4, 8 or 16)
+    int ns;   // component groups per CTA (1 or 3)
+};
+// Lane split for C components; max_cc caps components per CTA (shared-memory bound).
+CompSplit choose_comp_split(int C, int max_cc);
+size_t spread_smem_bytes(const MeshGeom &g, size_t elem, CompSplit cs);
+constexpr size_t kSpreadSmemCap = 200 * 1024;
+template <typename T>
+cudaError_t launch_spread(const int *tile_off, const int *rec_idx, const uint32_t *rec_start,
+                          const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
+                          cudaStream_t s);
+template <typename T>
+cudaError_t launch_interp(int n, const int *rec_idx, const uint32_t *rec_start,
+                          const T *rec_w, const T *mesh, int C, const MeshGeom &g, T *W,
+                          int accumulate, cudaStream_t s);
+
+// ---- k-space influence (influence.cu) -------------------------------------
+// tab[(z*K + y)*Kh + kx] = (S(k)|b|^2 / V, S(k)|b|^2 / (V k^2)), zero at k = 0.
+template <typename T>
+void launch_influence_table(T *tab2, const double *bmod2, int K, double L, double xi,
+                            double a, cudaStream_t s);
+// In-place influence on the interleaved half spectrum G[(z*K+y)*Kh+kx][C].
+template <typename T>
+void launch_influence(T *G, const T *tab2, int K, double L, int R, cudaStream_t s);
+
+// ---- real-space pair sum + self term (realspace.cu) -----------------------
+template <typename T>
+cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm,
+                             const double4 *cpos, const T *F, int R, double L, double rc,
+                             double xi, double a, int with_real, int with_self, T *W,
+                             cudaStream_t s);
+
+// ---- layout conversions (pack.cu) -----------------------------------------
+// W = self_c * F (the self term alone, when no real-space sum is requested)
+template <typename T>
+void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s);
+// F[i][3R] = f[r*ld + 3i + d]
+template <typename T>
+void launch_pack(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
+// u[r*ld + 3i + d] = beta*u + alpha*W[i][3r+d]   (u not read when beta == 0)
+template <typename T>
+void launch_unpack(const T *W, int n, int R, double alpha, double beta, T *u, long ld,
+                   cudaStream_t s);
+
+}  // namespace spme

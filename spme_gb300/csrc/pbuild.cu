@@ -1,0 +1,235 @@
+// P-build: stencil starts, tile / cell keys, counting sorts and B-spline
+// records (restates old-version/spme.c:158-297 in factored form: p weights per
+// axis instead of the dense p^3 P matrix and index list).
+#include "kernels.h"
+
+namespace spme {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void k_tile_keys(const double *__restrict__ pos, int n, MeshGeom g,
+                            int *__restrict__ key, int *__restrict__ count,
+                            int *__restrict__ slot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double fr;
+        mesh_coord(pos[3 * i + d], g.L, g.K, g.p, s[d], fr);
+    }
+    int k = ((s[2] / g.tz) * g.nty + s[1] / g.ty) * g.ntx + s[0] / g.tx;
+    key[i] = k;
+    slot[i] = atomicAdd(&count[k], 1);
+}
+
+__global__ void k_cell_keys(const double *__restrict__ pos, int n, double L, int nc,
+                            int *__restrict__ key, int *__restrict__ count,
+                            int *__restrict__ slot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double x = pos[3 * i + d];
+        x -= L * floor(x / L);
+        int v = (int)(x / L * (double)nc);
+        c[d] = v >= nc ? nc - 1 : v;
+    }
+    int k = (c[2] * nc + c[1]) * nc + c[0];
+    key[i] = k;
+    slot[i] = atomicAdd(&count[k], 1);
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ int block_exclusive_scan(int v, int &total) {
+    __shared__ int warp_tot[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+        int t = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) warp_tot[lane] = t;  // inclusive
+    }
+    __syncthreads();
+    int before = warp > 0 ? warp_tot[warp - 1] : 0;
+    total = warp_tot[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int *__restrict__ in, int n,
+                                                             int *__restrict__ sums) {
+    long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < n) s += in[base + k];
+    int total;
+    block_exclusive_scan(s, total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of sums[0..nb) in place, one block, looping with a carry.
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(int *__restrict__ sums, int nb) {
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += kScanTile) {
+        int v[kScanItems];
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            int q = base + threadIdx.x * kScanItems + k;
+            v[k] = q < nb ? sums[q] : 0;
+            s += v[k];
+        }
+        int total;
+        int ex = block_exclusive_scan(s, total) + carry;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            int q = base + threadIdx.x * kScanItems + k;
+            if (q < nb) sums[q] = ex;
+            ex += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(const int *__restrict__ in, int n,
+                                                            const int *__restrict__ sums,
+                                                            int *__restrict__ out) {
+    long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int ex = block_exclusive_scan(s, total) + sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < n) out[base + k] = ex;
+        ex += v[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = ex;
+}
+
+__global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ slot,
+                          const int *__restrict__ off, int n, int *__restrict__ perm) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    perm[off[key[i]] + slot[i]] = i;
+}
+
+template <typename T, int P>
+__global__ void k_records(const double *__restrict__ pos, const int *__restrict__ perm, int n,
+                          MeshGeom g, int *__restrict__ rec_idx,
+                          uint32_t *__restrict__ rec_start, T *__restrict__ rec_w) {
+    constexpr int WS = RecordWidth<T, P>::value;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int i = perm[s];
+    int st[3];
+    T w[3][P];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double fr;
+        mesh_coord(pos[3 * i + d], g.L, g.K, P, st[d], fr);
+        bspline_weights<T, P>((T)fr, w[d]);
+    }
+    rec_idx[s] = i;
+    rec_start[s] = pack_start(st[0], st[1], st[2]);
+    T *out = rec_w + (size_t)s * WS;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int j = 0; j < P; j++) out[d * P + j] = w[d][j];
+#pragma unroll
+    for (int j = 3 * P; j < WS; j++) out[j] = T(0);
+}
+
+__global__ void k_cell_positions(const double *__restrict__ pos, const int *__restrict__ perm,
+                                 int n, double L, double4 *__restrict__ cpos) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int i = perm[s];
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    x -= L * floor(x / L);
+    y -= L * floor(y / L);
+    z -= L * floor(z / L);
+    cpos[s] = make_double4(x, y, z, 0.0);
+}
+
+inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+void launch_tile_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
+                      int *slot, cudaStream_t s) {
+    if (n > 0) k_tile_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, key, count, slot);
+}
+
+void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
+                      int *slot, cudaStream_t s) {
+    if (n > 0) k_cell_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, L, nc, key, count, slot);
+}
+
+size_t scan_tmp_elems(int nkeys) { return (size_t)nblk(nkeys, kScanTile) + 1; }
+
+void launch_scan(const int *count, int nkeys, int *off, int *tmp, cudaStream_t s) {
+    int nb = nblk(nkeys, kScanTile);
+    if (nb < 1) nb = 1;
+    k_scan_reduce<<<nb, kScanThreads, 0, s>>>(count, nkeys, tmp);
+    k_scan_sums<<<1, kScanThreads, 0, s>>>(tmp, nb);
+    k_scan_final<<<nb, kScanThreads, 0, s>>>(count, nkeys, tmp, off);
+}
+
+void launch_scatter(const int *key, const int *slot, const int *off, int n, int *perm,
+                    cudaStream_t s) {
+    if (n > 0) k_scatter<<<nblk(n, 256), 256, 0, s>>>(key, slot, off, n, perm);
+}
+
+template <typename T>
+void launch_records(const double *pos, const int *perm, int n, const MeshGeom &g,
+                    int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s) {
+    if (n <= 0) return;
+    switch (g.p) {
+        case 4: k_records<T, 4><<<nblk(n, 128), 128, 0, s>>>(pos, perm, n, g, rec_idx, rec_start, rec_w); break;
+        case 6: k_records<T, 6><<<nblk(n, 128), 128, 0, s>>>(pos, perm, n, g, rec_idx, rec_start, rec_w); break;
+        case 8: k_records<T, 8><<<nblk(n, 128), 128, 0, s>>>(pos, perm, n, g, rec_idx, rec_start, rec_w); break;
+        default: break;
+    }
+}
+
+void launch_cell_positions(const double *pos, const int *perm, int n, double L,
+                           double4 *cpos, cudaStream_t s) {
+    if (n > 0) k_cell_positions<<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, cpos);
+}
+
+template void launch_records<float>(const double *, const int *, int, const MeshGeom &, int *,
+                                    uint32_t *, float *, cudaStream_t);
+template void launch_records<double>(const double *, const int *, int, const MeshGeom &, int *,
+                                     uint32_t *, double *, cudaStream_t);
+
+}  // namespace spme

@@ -1,0 +1,169 @@
+"""GPU parity: the sm_103a path (through the C ABI) against the reference's
+golden vectors and the oracle.  Tolerances: FP64 <= 1e-12 relative L2
+(reference and oracle), FP32 batched <= 1e-5 relative L2 vs the FP64 oracle."""
+import numpy as np
+import pytest
+
+import oracle
+import spme_gb300
+from conftest import GOLDEN_CASES, load_golden, relerr, uniform_case
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-5
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_dropin_matches_reference_golden(gpu_lib, name):
+    g = load_golden(name)
+    n = g["pos"].shape[0]
+    nrhs = g["f"].shape[0]
+    h = spme_gb300.create_spme_engine(g["xi"], int(g["K"]), int(g["p"]), n, g["L"], 1)
+    try:
+        vout = g["v0"].copy()
+        spme_gb300.compute_spme(h, g["pos"], nrhs, g["alpha"], g["f"], 3 * n, g["beta"], vout,
+                                3 * n)
+        assert relerr(vout, g["vout"]) < FP64_TOL
+        part = vout - g["beta"] * g["v0"]
+        assert relerr(part, g["vout"] - g["beta"] * g["v0"]) < FP64_TOL
+        # pos == NULL reuses the positions
+        vout2 = g["v0"].copy()
+        spme_gb300.compute_spme(h, None, nrhs, g["alpha"], g["f"], 3 * n, g["beta"], vout2,
+                                3 * n)
+        assert relerr(vout2, g["vout"]) < FP64_TOL
+    finally:
+        spme_gb300.destroy_spme_engine(h)
+
+
+def test_dropin_leading_dimensions(gpu_lib):
+    g = load_golden("n300_k32_p6")
+    n, nrhs = g["pos"].shape[0], g["f"].shape[0]
+    ld = 3 * n + 7
+    fin = np.zeros((nrhs, ld))
+    fin[:, :3 * n] = g["f"]
+    vout = np.full((nrhs, ld), 99.0)
+    vout[:, :3 * n] = g["v0"]
+    h = spme_gb300.create_spme_engine(g["xi"], int(g["K"]), int(g["p"]), n, g["L"], 1)
+    try:
+        spme_gb300.compute_spme(h, g["pos"], nrhs, g["alpha"], fin, ld, g["beta"], vout, ld)
+    finally:
+        spme_gb300.destroy_spme_engine(h)
+    assert relerr(vout[:, :3 * n], g["vout"]) < FP64_TOL
+    assert np.all(vout[:, 3 * n:] == 99.0)  # padding untouched
+
+
+# (N, L, K, p, xi): odd / 5-smooth K, p = 8, 4p >= K, K not a multiple of the tile
+RECIP_CASES = [
+    (257, 20.0, 25, 4, 0.5),
+    (300, 30.0, 27, 6, 0.4),
+    (500, 40.0, 45, 8, 0.3),
+    (200, 12.0, 24, 8, 0.6),
+    (1000, 50.0, 60, 6, 0.3),
+    (128, 16.0, 8, 4, 0.9),
+    (999, 35.0, 36, 6, 0.35),
+]
+
+
+@pytest.mark.parametrize("case", RECIP_CASES)
+def test_recip_fp64_vs_oracle(gpu_lib, case):
+    n, L, K, p, xi = case
+    pos, f = uniform_case(n, L, 2, seed=n + K)
+    eng = spme_gb300.Engine(n, L, xi, K, p, precision="fp64", max_nrhs=2,
+                            terms=spme_gb300.TERM_RECIP)
+    eng.set_positions(pos)
+    u = eng.apply(f, alpha=1.3)
+    ref = oracle.recip(pos, L, xi, K, p, f, alpha=1.3, nthreads=4)
+    assert relerr(u, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("tile", [(4, 4, 4), (8, 8, 8), (16, 8, 4), (16, 16, 16)])
+def test_tile_shapes(gpu_lib, tile):
+    n, L, K, p, xi = 700, 30.0, 40, 6, 0.4
+    pos, f = uniform_case(n, L, 3, seed=5)
+    eng = spme_gb300.Engine(n, L, xi, K, p, precision="fp64", max_nrhs=3,
+                            terms=spme_gb300.TERM_RECIP, tile=tile)
+    eng.set_positions(pos)
+    u = eng.apply(f)
+    ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
+    assert relerr(u, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("radius", [1.0, 1.5])
+def test_full_operator_fp64_vs_oracle(gpu_lib, radius):
+    n, L, K, p, xi, rc = 2000, 50.0, 64, 6, 0.3, 10.0
+    pos, f = uniform_case(n, L, 2, seed=77)
+    eng = spme_gb300.Engine(n, L, xi, K, p, radius=radius, rcut=rc, precision="fp64",
+                            max_nrhs=2, terms=spme_gb300.TERM_ALL)
+    eng.set_positions(pos)
+    u0 = np.random.default_rng(1).standard_normal(f.shape)
+    u = eng.apply(f, u=u0.copy(), alpha=0.7, beta=-0.4)
+    ref = oracle.full(pos, L, xi, rc, K, p, f, alpha=0.7, beta=-0.4, u=u0, radius=radius,
+                      nthreads=4)
+    assert relerr(u, ref) < FP64_TOL
+
+
+def test_real_and_self_terms_separately(gpu_lib):
+    n, L, K, p, xi, rc = 1500, 40.0, 32, 4, 0.35, 9.0
+    pos, f = uniform_case(n, L, 1, seed=8)
+    for terms, kw in ((spme_gb300.TERM_REAL, dict(real=True, self_term=False)),
+                      (spme_gb300.TERM_SELF, dict(real=False, self_term=True))):
+        eng = spme_gb300.Engine(n, L, xi, K, p, rcut=rc, terms=terms)
+        eng.set_positions(pos)
+        u = eng.apply(f)
+        ref = oracle.real_self(pos, L, xi, rc, f, nthreads=4, **kw)
+        assert relerr(u, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("nrhs,max_nrhs", [(16, 16), (5, 4), (1, 1)])
+def test_fp32_batched_vs_fp64_oracle(gpu_lib, nrhs, max_nrhs):
+    n, L, K, p, xi, rc = 3000, 60.0, 64, 6, 0.3, 10.0
+    pos, f = uniform_case(n, L, nrhs, seed=3)
+    eng = spme_gb300.Engine(n, L, xi, K, p, rcut=rc, precision="fp32", max_nrhs=max_nrhs,
+                            terms=spme_gb300.TERM_ALL)
+    eng.set_positions(pos)
+    u = eng.apply(f.astype(np.float32))
+    ref = oracle.full(pos, L, xi, rc, K, p, f, nthreads=4)
+    err = relerr(u, ref)
+    assert err < FP32_TOL, err
+
+
+def test_edge_cases(gpu_lib):
+    # one particle; particles on the box faces and outside [0, L) (wrapped)
+    L, K, p, xi = 10.0, 16, 4, 0.5
+    pos = np.array([[0.0, 0.0, 0.0], [L * (1 - 1e-16), 5.0, 9.999999999], [-3.0, 12.5, 4.0]])
+    f = np.random.default_rng(0).standard_normal((1, 9))
+    eng = spme_gb300.Engine(3, L, xi, K, p, terms=spme_gb300.TERM_RECIP)
+    eng.set_positions(pos)
+    u = eng.apply(f)
+    ref = oracle.recip(np.mod(pos, L), L, xi, K, p, f, nthreads=1)
+    assert relerr(u, ref) < FP64_TOL
+    # nrhs == 0 is a no-op
+    out = np.ones((1, 9))
+    eng.apply(np.zeros((0, 9)), u=np.zeros((0, 9)))
+    assert np.all(out == 1.0)
+    # a single particle
+    e1 = spme_gb300.Engine(1, L, xi, K, p, terms=spme_gb300.TERM_RECIP)
+    e1.set_positions(pos[:1])
+    u1 = e1.apply(f[:, :3])
+    assert relerr(u1, oracle.recip(pos[:1], L, xi, K, p, f[:, :3], nthreads=1)) < FP64_TOL
+
+
+def test_apply_before_positions_is_an_error(gpu_lib):
+    eng = spme_gb300.Engine(10, 10.0, 0.5, 16, 4, terms=spme_gb300.TERM_RECIP)
+    with pytest.raises(spme_gb300.SpmeError):
+        eng.apply(np.zeros((1, 30)))
+
+
+def test_device_pointer_api(gpu_lib):
+    import torch
+    n, L, K, p, xi, rc = 1200, 40.0, 32, 6, 0.35, 9.0
+    pos, f = uniform_case(n, L, 4, seed=12)
+    eng = spme_gb300.Engine(n, L, xi, K, p, rcut=rc, precision="fp32", max_nrhs=4)
+    eng.set_positions(torch.tensor(pos, device="cuda"))
+    fd = torch.tensor(f, dtype=torch.float32, device="cuda")
+    ud = torch.zeros_like(fd)
+    eng.apply(fd, ud)
+    eng.synchronize()
+    ref = oracle.full(pos, L, xi, rc, K, p, f, nthreads=4)
+    assert relerr(ud.cpu().numpy(), ref) < FP32_TOL
