@@ -98,19 +98,23 @@ int spme_apply(spme_t *spme, int nrhs, double alpha, const void *f, long ldf, do
 /* Block until the engine's stream is idle. */
 int spme_synchronize(spme_t *spme);
 
-/* Per-stage device times (ms) of the last apply when profiling is on
- * (spme_set_profiling(spme, 1)).  Stages, in order: pack, real-space,
- * spread, forward FFT, influence, backward FFT, interpolate, unpack.
- * Returns the number of stages written (<= n). */
+/* Per-stage device times (ms) of the last apply when profiling is on.
+ * spme_set_profiling(spme, 1): CUDA events around each stage, the real-space
+ * sum still overlapping the mesh stages on its own stream; level 2 also runs
+ * the real-space sum on the main stream so each stage is timed alone; 0 off.
+ * Stages, in order: pack, real-space, spread, forward FFT, influence,
+ * backward FFT, interpolate, unpack.  Returns the number of stages written
+ * (<= n). */
 int spme_set_profiling(spme_t *spme, int on);
 int spme_stage_times(const spme_t *spme, float *ms, int n);
 
-/* Number of kernels this engine launched since creation (cuFFT launches
- * counted as the plan's kernels are not visible here: one per FFT call). */
+/* Number of this library's kernels the engine has launched since creation
+ * (cuFFT's own kernels are not included). */
 long spme_launch_count(const spme_t *spme);
 
-/* Mesh-tile shape used by spread/interpolate (default 8 x 8 x 8; each 1..16).
- * Takes effect at the next spme_set_positions. */
+/* Mesh-tile shape used by spread/interpolate (default 8 x 8 x 8; tx, ty in
+ * 4..16, tz in 4..8).  Takes effect at the next spme_set_positions, which must
+ * follow before the next apply. */
 int spme_set_tile(spme_t *spme, int tx, int ty, int tz);
 
 #ifdef __cplusplus

@@ -250,8 +250,9 @@ class Engine:
     def synchronize(self):
         _check(load().spme_synchronize(self.h), "spme_synchronize")
 
-    def set_profiling(self, on: bool = True):
-        load().spme_set_profiling(self.h, 1 if on else 0)
+    def set_profiling(self, level: int = 1):
+        """0 off; 1 stage events (real-space still overlapped); 2 stages serialized."""
+        load().spme_set_profiling(self.h, int(level))
 
     def stage_times(self) -> dict:
         buf = (ctypes.c_float * len(STAGES))()

@@ -76,6 +76,25 @@ __device__ __forceinline__ void unpack_start(uint32_t v, int &sx, int &sy, int &
     sz = (int)((v >> 20) & 1023u);
 }
 
+// q / d and q % d for 0 <= q < 2^22, 0 < d < 2^10 via a float reciprocal
+// (exact after one correction step).
+struct DivMod {
+    int d;
+    float inv;
+    __device__ __forceinline__ void init(int dd) {
+        d = dd;
+        inv = 1.0f / (float)dd;
+    }
+    __device__ __forceinline__ int div(int q, int &rem) const {
+        int qd = (int)((float)q * inv);
+        int r = q - qd * d;
+        if (r < 0) { qd--; r += d; }
+        if (r >= d) { qd++; r -= d; }
+        rem = r;
+        return qd;
+    }
+};
+
 template <typename T> struct Vec2;
 template <> struct Vec2<float> { using type = float2; };
 template <> struct Vec2<double> { using type = double2; };

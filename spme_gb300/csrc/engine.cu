@@ -1,6 +1,7 @@
 // Host engine and C ABI of the GB300 SPME-RPY mobility operator.
 //
-// Orchestrates, per mesh pass of R right-hand sides (C = 3R components):
+// Orchestrates, per mesh pass of R right-hand sides (C = 3R components, mesh
+// stored component-major so cuFFT runs contiguous batched transforms):
 //   pack -> [aux stream: real-space + self] -> spread -> cuFFT R2C ->
 //   influence -> cuFFT C2R -> interpolate (+ real-space result) -> unpack
 // The reference's compute_spme (old-version/spme.c:560-726) runs the whole
@@ -28,6 +29,8 @@ struct PlanPair {
     int C;
     cufftHandle fwd;
     cufftHandle bwd;
+    spme::InterpMaps maps;  // TMA boxes over the mesh for this C and tile shape
+    int maps_tile[3];
 };
 
 }  // namespace
@@ -38,7 +41,7 @@ struct _spme_t {
     int last_error = SPME_OK;
     cudaStream_t own_stream = nullptr, stream = nullptr, aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    bool profiling = false;
+    int profiling = 0;  // 1: stage events; 2: events + real-space serialized
     cudaEvent_t ev[kStages + 1] = {};
     cudaEvent_t ev_rs[2] = {};
     float stage_ms[kStages] = {};
@@ -60,13 +63,14 @@ struct _spme_t {
     uint32_t *d_rec_start = nullptr;
     void *d_rec_w = nullptr;
     int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
-    double4 *d_cpos = nullptr;
+    void *d_cpos = nullptr;  // float4 (FP32 engine) or double4 (FP64 engine)
     void *d_mesh = nullptr, *d_cmesh = nullptr, *d_tab = nullptr;
     double *d_bmod2 = nullptr;
     void *d_work = nullptr;
     size_t work_bytes = 0;
     std::vector<PlanPair> plans;
     void *d_F = nullptr, *d_W = nullptr, *d_fstage = nullptr, *d_ustage = nullptr;
+    int *d_err = nullptr;  // device-side error flag (TMA wait timeouts)
     size_t cap_tiles = 0;  // allocated tile-count capacity
 };
 
@@ -227,6 +231,7 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
     int n[3] = {K, K, K}, re[3] = {K, K, K}, ce[3] = {K, K, K / 2 + 1};
     PlanPair pp;
     pp.C = C;
+    pp.maps_tile[0] = pp.maps_tile[1] = pp.maps_tile[2] = 0;
     size_t ws1 = 0, ws2 = 0;
     TRY_FFT(cufftCreate(&pp.fwd));
     TRY_FFT(cufftCreate(&pp.bwd));
@@ -234,8 +239,10 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
     TRY_FFT(cufftSetAutoAllocation(pp.bwd, 0));
     cufftType tf = is_fp32(e) ? CUFFT_R2C : CUFFT_D2Z;
     cufftType tb = is_fp32(e) ? CUFFT_C2R : CUFFT_Z2D;
-    TRY_FFT(cufftMakePlanMany(pp.fwd, 3, n, re, C, 1, ce, C, 1, tf, C, &ws1));
-    TRY_FFT(cufftMakePlanMany(pp.bwd, 3, n, ce, C, 1, re, C, 1, tb, C, &ws2));
+    // component-major: batch b of the real mesh at b*K^3, of the half spectrum at b*Kc
+    const long long K3 = (long long)K * K * K, Kc = (long long)K * K * (K / 2 + 1);
+    TRY_FFT(cufftMakePlanMany(pp.fwd, 3, n, re, 1, (int)K3, ce, 1, (int)Kc, tf, C, &ws1));
+    TRY_FFT(cufftMakePlanMany(pp.bwd, 3, n, ce, 1, (int)Kc, re, 1, (int)K3, tb, C, &ws2));
     size_t ws = std::max(ws1, ws2);
     if (ws > e->work_bytes) {
         dfree(e->d_work);
@@ -319,6 +326,8 @@ int create_impl(const spme_params &prm, spme_t **out) {
         PlanPair *pp;
         TRY(get_plans(e, (int)C, &pp));
     }
+    TRY(dalloc(&e->d_err, sizeof(int)));
+    TRY_CUDA(cudaMemsetAsync(e->d_err, 0, sizeof(int), e->stream));
     TRY(dalloc(&e->d_F, e->elem * n * C));
     TRY(dalloc(&e->d_W, e->elem * n * C));
     TRY(dalloc(&e->d_fstage, e->elem * n * C));
@@ -340,7 +349,7 @@ void destroy_impl(spme_t *e) {
                     e->d_tperm,  e->d_scan_tmp, e->d_rec_idx, e->d_rec_start, e->d_rec_w,
                     e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_mesh,
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
-                    e->d_W,      e->d_fstage,  e->d_ustage};
+                    e->d_W,      e->d_fstage,  e->d_ustage, e->d_err};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -385,7 +394,8 @@ int set_positions_impl(spme_t *e, const double *pos, int mem) {
                                e->d_slot, s);
         spme::launch_scan(e->d_ccount, ncell, e->d_coff, e->d_scan_tmp, s);
         spme::launch_scatter(e->d_key, e->d_slot, e->d_coff, n, e->d_cperm, s);
-        spme::launch_cell_positions(e->d_pos, e->d_cperm, n, e->prm.box_size, e->d_cpos, s);
+        spme::launch_cell_positions(e->d_pos, e->d_cperm, n, e->prm.box_size, e->nc, is_fp32(e),
+                                    e->d_cpos, s);
         e->launches += 6;
     }
     TRY_CUDA(cudaGetLastError());
@@ -405,22 +415,29 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
     spme::launch_pack<T>(f, ldf, n, R, F, s);
     e->launches++;
     if (prof) cudaEventRecord(e->ev[1], s);
+    // the real-space sum overlaps the mesh pipeline on the aux stream; at
+    // profiling level 2 it runs on the main stream so every stage is timed alone
+    const bool serial = e->profiling >= 2;
+    cudaStream_t rss = serial ? s : e->aux;
     if (rs) {
-        TRY_CUDA(cudaEventRecord(e->ev_fork, s));
-        TRY_CUDA(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
-        if (prof) cudaEventRecord(e->ev_rs[0], e->aux);
+        if (!serial) {
+            TRY_CUDA(cudaEventRecord(e->ev_fork, s));
+            TRY_CUDA(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
+        }
+        if (prof) cudaEventRecord(e->ev_rs[0], rss);
         if (terms & SPME_TERM_REAL) {
             if (!e->d_coff || !e->d_cperm || !e->d_cpos) return SPME_ERR_STATE;
             TRY_CUDA(spme::launch_realspace<T>(e->nc, e->d_coff, e->d_cperm, e->d_cpos, F, R,
                                                e->prm.box_size, e->prm.rcut, e->prm.xi,
-                                               e->prm.radius, 1,
-                                               (terms & SPME_TERM_SELF) ? 1 : 0, W, e->aux));
+                                               e->prm.radius, (terms & SPME_TERM_SELF) ? 1 : 0,
+                                               W, rss));
         } else {
-            spme::launch_self<T>(F, n, R, self_coeff(e->prm.xi, e->prm.radius), W, e->aux);
+            spme::launch_self<T>(F, n, R, self_coeff(e->prm.xi, e->prm.radius), W, rss);
         }
         e->launches++;
-        if (prof) cudaEventRecord(e->ev_rs[1], e->aux);
-        TRY_CUDA(cudaEventRecord(e->ev_join, e->aux));
+        if (prof) cudaEventRecord(e->ev_rs[1], rss);
+        TRY_CUDA(cudaEventRecord(e->ev_join, rss));
+        if (serial) cudaEventRecord(e->ev[1], s);
     }
     if (terms & SPME_TERM_RECIP) {
         if (!e->d_mesh || !e->d_cmesh || !e->d_tab) return SPME_ERR_STATE;
@@ -446,8 +463,16 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
                                  (cufftDoubleReal *)e->d_mesh));
         if (prof) cudaEventRecord(e->ev[5], s);
         if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
-        TRY_CUDA(spme::launch_interp<T>(n, e->d_rec_idx, e->d_rec_start, (const T *)e->d_rec_w,
-                                        (const T *)e->d_mesh, C, e->g, W, rs ? 1 : 0, s));
+        if (pp->maps_tile[0] != e->g.tx || pp->maps_tile[1] != e->g.ty ||
+            pp->maps_tile[2] != e->g.tz) {
+            spme::make_interp_maps(&pp->maps, e->d_mesh, C, e->g, e->elem);
+            pp->maps_tile[0] = e->g.tx;
+            pp->maps_tile[1] = e->g.ty;
+            pp->maps_tile[2] = e->g.tz;
+        }
+        TRY_CUDA(spme::launch_interp<T>(pp->maps, e->d_toff, n, e->d_rec_idx, e->d_rec_start,
+                                        (const T *)e->d_rec_w, (const T *)e->d_mesh, C, e->g, W,
+                                        rs ? 1 : 0, e->d_err, s));
         e->launches++;
         if (prof) cudaEventRecord(e->ev[6], s);
     } else {
@@ -461,6 +486,17 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
     e->ran_real = rs;
     e->stages_valid = prof;
     return from_cuda(cudaGetLastError());
+}
+
+// A device-side check (bounded TMA wait) failed: report it once and clear.
+int check_device_error(spme_t *e) {
+    int h = 0;
+    TRY_CUDA(cudaMemcpy(&h, e->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        TRY_CUDA(cudaMemset(e->d_err, 0, sizeof(int)));
+        return SPME_ERR_KERNEL;
+    }
+    return SPME_OK;
 }
 
 int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, double beta, void *u,
@@ -500,7 +536,10 @@ int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
             TRY(st);
         }
     }
-    if (mem == SPME_MEM_HOST) TRY_CUDA(cudaStreamSynchronize(e->stream));
+    if (mem == SPME_MEM_HOST) {
+        TRY_CUDA(cudaStreamSynchronize(e->stream));
+        TRY(check_device_error(e));
+    }
     return SPME_OK;
 }
 
@@ -563,12 +602,14 @@ int spme_apply(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
 int spme_synchronize(spme_t *e) {
     if (!e) return SPME_ERR_INVALID;
     DeviceGuard dg(e->device);
-    return e->last_error = from_cuda(cudaStreamSynchronize(e->stream));
+    int st = from_cuda(cudaStreamSynchronize(e->stream));
+    if (st == SPME_OK) st = check_device_error(e);
+    return e->last_error = st;
 }
 
 int spme_set_profiling(spme_t *e, int on) {
     if (!e) return SPME_ERR_INVALID;
-    e->profiling = on != 0;
+    e->profiling = on < 0 ? 0 : (on > 2 ? 2 : on);
     e->stages_valid = false;
     return SPME_OK;
 }
@@ -593,9 +634,16 @@ long spme_launch_count(const spme_t *e) { return e ? e->launches : 0; }
 
 int spme_set_tile(spme_t *e, int tx, int ty, int tz) {
     if (!e) return SPME_ERR_INVALID;
-    if (tx < 4 || ty < 4 || tz < 4 || tx > spme::kMaxTile || ty > spme::kMaxTile ||
-        tz > spme::kMaxTile)
+    if (tx < 4 || ty < 4 || tz < 4 || tx > spme::kMaxTile || ty > spme::kMaxTile || tz > 8)
         return e->last_error = SPME_ERR_INVALID;
+    // the interpolation kernel stages the tile plus its (p - 1) halo for at
+    // least 4 components in shared memory
+    MeshGeom g = e->g;
+    g.tx = tx;
+    g.ty = ty;
+    g.tz = tz;
+    if (spme::interp_smem_bytes(g, e->elem) > 220 * 1024)
+        return e->last_error = SPME_ERR_UNSUPPORTED;
     e->tile[0] = tx;
     e->tile[1] = ty;
     e->tile[2] = tz;

@@ -13,6 +13,9 @@
 // transform then keeps the real part of the inverse transform along y and z.
 // This kernel produces the Hermitian part directly (pairing (y,z) with
 // (-y,-z)), which gives any C2R implementation the same result.
+//
+// Layout: component-major half spectrum G[c][(z*K + y)*Kh + kx], c = 3r + d,
+// the contiguous batched layout of the cuFFT R2C/C2R plans.
 #include "kernels.h"
 
 namespace spme {
@@ -74,17 +77,16 @@ __device__ __forceinline__ void apply_B(T m2, T c, T kx, T ky, T kz, const Cx<T>
 }
 
 // All planes x in [1, K/2) (even K) or [1, K/2] (odd K): independent points.
+// Component-major half spectrum G[c][kidx], c = 3r + d; one thread per k-point
+// reads its table entry once and streams all R right-hand sides.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_influence(Cx<T> *__restrict__ G, const T *__restrict__ tab2, int K, T twopi_L, int R) {
     using V2 = typename Vec2<T>::type;
     const int Kh = K / 2 + 1;
-    const size_t total = (size_t)K * K * Kh * R;
-    const int C = 3 * R;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const int r = (int)(t % R);
-        const size_t kidx = t / R;
+    const size_t Kc = (size_t)K * K * Kh;
+    for (size_t kidx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; kidx < Kc;
+         kidx += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(kidx % Kh);
         if (x == 0 || (!(K & 1) && x == K / 2)) continue;
         const size_t rest = kidx / Kh;
@@ -93,12 +95,25 @@ k_influence(Cx<T> *__restrict__ G, const T *__restrict__ tab2, int K, T twopi_L,
         const T kx = (T)(x <= K / 2 ? x : x - K) * twopi_L;
         const T ky = (T)(y <= K / 2 ? y : y - K) * twopi_L;
         const T kz = (T)(z <= K / 2 ? z : z - K) * twopi_L;
-        Cx<T> *p = G + kidx * C + 3 * r;
-        Cx<T> g[3] = {p[0], p[1], p[2]}, o[3];
-        apply_B<T>(mc.x, mc.y, kx, ky, kz, g, o);
-        p[0] = o[0];
-        p[1] = o[1];
-        p[2] = o[2];
+        const T m2 = mc.x, c = mc.y;
+        const T b0 = m2 - c * kx * kx, b1 = -c * kx * ky, b2 = -c * kx * kz;
+        const T b3 = m2 - c * ky * ky, b4 = -c * ky * kz, b5 = m2 - c * kz * kz;
+        Cx<T> *p = G + kidx;
+#pragma unroll 4
+        for (int r = 0; r < R; r++) {
+            Cx<T> *q = p + (size_t)(3 * r) * Kc;
+            const Cx<T> g0 = q[0], g1 = q[Kc], g2 = q[2 * Kc];
+            Cx<T> o;
+            o.re = b0 * g0.re + b1 * g1.re + b2 * g2.re;
+            o.im = b0 * g0.im + b1 * g1.im + b2 * g2.im;
+            q[0] = o;
+            o.re = b1 * g0.re + b3 * g1.re + b4 * g2.re;
+            o.im = b1 * g0.im + b3 * g1.im + b4 * g2.im;
+            q[Kc] = o;
+            o.re = b2 * g0.re + b4 * g1.re + b5 * g2.re;
+            o.im = b2 * g0.im + b4 * g1.im + b5 * g2.im;
+            q[2 * Kc] = o;
+        }
     }
 }
 
@@ -109,14 +124,13 @@ __global__ void __launch_bounds__(256)
 k_influence_planes(Cx<T> *__restrict__ G, const T *__restrict__ tab2, int K, T twopi_L, int R) {
     using V2 = typename Vec2<T>::type;
     const int Kh = K / 2 + 1;
+    const size_t Kc = (size_t)K * K * Kh;
     const int nplanes = (K & 1) ? 1 : 2;
-    const size_t total = (size_t)nplanes * K * K * R;
-    const int C = 3 * R;
+    const size_t total = (size_t)nplanes * K * K;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x) {
-        const int r = (int)(t % R);
-        const size_t q = (t / R) % ((size_t)K * K);
-        const int pl = (int)(t / ((size_t)R * K * K));
+        const size_t q = t % ((size_t)K * K);
+        const int pl = (int)(t / ((size_t)K * K));
         const int x = pl == 0 ? 0 : K / 2;
         const int y = (int)(q % K), z = (int)(q / K);
         const int y2 = (K - y) % K, z2 = (K - z) % K;
@@ -124,32 +138,34 @@ k_influence_planes(Cx<T> *__restrict__ G, const T *__restrict__ tab2, int K, T t
         if (q > q2) continue;
         const T kx = (T)(x <= K / 2 ? x : x - K) * twopi_L;
         const size_t k1 = q * Kh + x, k2 = q2 * Kh + x;
-        Cx<T> *p1 = G + k1 * C + 3 * r;
-        Cx<T> *p2 = G + k2 * C + 3 * r;
-        Cx<T> g1[3] = {p1[0], p1[1], p1[2]}, o1[3];
         const V2 mc1 = reinterpret_cast<const V2 *>(tab2)[k1];
-        apply_B<T>(mc1.x, mc1.y, kx, (T)(y <= K / 2 ? y : y - K) * twopi_L,
-                   (T)(z <= K / 2 ? z : z - K) * twopi_L, g1, o1);
-        if (q == q2) {
+        const V2 mc2 = reinterpret_cast<const V2 *>(tab2)[k2];
+        const T ky1 = (T)(y <= K / 2 ? y : y - K) * twopi_L, kz1 = (T)(z <= K / 2 ? z : z - K) * twopi_L;
+        const T ky2 = (T)(y2 <= K / 2 ? y2 : y2 - K) * twopi_L, kz2 = (T)(z2 <= K / 2 ? z2 : z2 - K) * twopi_L;
+        for (int r = 0; r < R; r++) {
+            Cx<T> *p1 = G + (size_t)(3 * r) * Kc + k1;
+            Cx<T> *p2 = G + (size_t)(3 * r) * Kc + k2;
+            Cx<T> g1[3] = {p1[0], p1[Kc], p1[2 * Kc]}, o1[3];
+            apply_B<T>(mc1.x, mc1.y, kx, ky1, kz1, g1, o1);
+            if (q == q2) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    o1[d].im = T(0);
+                    p1[d * Kc] = o1[d];
+                }
+                continue;
+            }
+            Cx<T> g2[3] = {p2[0], p2[Kc], p2[2 * Kc]}, o2[3];
+            apply_B<T>(mc2.x, mc2.y, kx, ky2, kz2, g2, o2);
 #pragma unroll
             for (int d = 0; d < 3; d++) {
-                o1[d].im = T(0);
-                p1[d] = o1[d];
+                Cx<T> h;
+                h.re = T(0.5) * (o1[d].re + o2[d].re);
+                h.im = T(0.5) * (o1[d].im - o2[d].im);
+                p1[d * Kc] = h;
+                h.im = -h.im;
+                p2[d * Kc] = h;
             }
-            continue;
-        }
-        Cx<T> g2[3] = {p2[0], p2[1], p2[2]}, o2[3];
-        const V2 mc2 = reinterpret_cast<const V2 *>(tab2)[k2];
-        apply_B<T>(mc2.x, mc2.y, kx, (T)(y2 <= K / 2 ? y2 : y2 - K) * twopi_L,
-                   (T)(z2 <= K / 2 ? z2 : z2 - K) * twopi_L, g2, o2);
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            Cx<T> h;
-            h.re = T(0.5) * (o1[d].re + o2[d].re);
-            h.im = T(0.5) * (o1[d].im - o2[d].im);
-            p1[d] = h;
-            h.im = -h.im;
-            p2[d] = h;
         }
     }
 }
@@ -177,9 +193,9 @@ void launch_influence(T *G, const T *tab2, int K, double L, int R, cudaStream_t 
     const T twopi_L = (T)(2.0 * M_PI / L);
     const size_t Kh = K / 2 + 1;
     Cx<T> *g = reinterpret_cast<Cx<T> *>(G);
-    k_influence<T><<<grid_for((size_t)K * K * Kh * R, 256), 256, 0, s>>>(g, tab2, K, twopi_L, R);
+    k_influence<T><<<grid_for((size_t)K * K * Kh, 256), 256, 0, s>>>(g, tab2, K, twopi_L, R);
     const int nplanes = (K & 1) ? 1 : 2;
-    k_influence_planes<T><<<grid_for((size_t)nplanes * K * K * R, 256), 256, 0, s>>>(
+    k_influence_planes<T><<<grid_for((size_t)nplanes * K * K, 256), 256, 0, s>>>(
         g, tab2, K, twopi_L, R);
 }
 

@@ -1,146 +1,269 @@
 // Interpolation of the 3R mesh components back to the particles (restates
 // old-version/spme_kernel.c:8-70: v_i = sum_j P_ij grid[c][ind_ij]).
 //
-// One warp per particle, visited in tile-sorted order so that consecutive
-// warps read overlapping mesh neighbourhoods (L1/L2 reuse).  Lanes are
-// (x-slot, component) pairs: each load instruction reads C-contiguous runs of
-// the interleaved mesh [z][y][x][C]; the x-slots are summed with shuffles.
+// One CTA per mesh tile.  For CG components at a time it stages the tile
+// plus its (p-1) upper halo in shared memory as a dense box
+// [CG][HZB][HYB][HX] (HX = 24 wide: every lane's x offset fits, and the
+// component-plane stride is 24 (mod 32) words so the gather below is
+// bank-conflict free):
+//   * interior tiles: one TMA (cp.async.bulk.tensor) load per chunk,
+//     completing on an mbarrier (bounded wait, error flag on timeout);
+//   * tiles whose halo wraps the periodic boundary: 16-byte vector loads.
+// Each warp then interpolates the tile's own particles (sorted by stencil
+// start) from shared memory: lanes are (x offset 0..7, component 0..3)
+// pairs, the x offsets summed with shuffles.  Every particle is handled by
+// exactly one CTA; mesh values come from HBM about once and from L2 for the
+// halos.
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace spme {
 
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kHX = 24;  // staged row width (elements)
 
-template <typename T, int P, int CGP, int NS>
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+template <typename T, int P, int CG>
 __global__ void __launch_bounds__(kThreads)
-k_interp(int n, const int *__restrict__ rec_idx, const uint32_t *__restrict__ rec_start,
-         const T *__restrict__ rec_w, const T *__restrict__ mesh, int C, MeshGeom g,
-         T *__restrict__ W, int accumulate) {
+k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
+         const int *__restrict__ tile_off, const int *__restrict__ rec_idx,
+         const uint32_t *__restrict__ rec_start, const T *__restrict__ rec_w,
+         const T *__restrict__ mesh, int C, MeshGeom g, T *__restrict__ W, int accumulate,
+         int *__restrict__ err) {
+    using V = typename Vec16<T>::type;
+    constexpr int VW = Vec16<T>::n;
+    constexpr int NV = kHX / VW;  // vectors per staged row
     constexpr int WS = RecordWidth<T, P>::value;
-    constexpr int XS = 32 / CGP;
-    constexpr int CC = CGP * NS;
-    constexpr int XI = (P + XS - 1) / XS;  // x iterations per lane
-    const int lane = threadIdx.x & 31;
-    const int xs = lane / CGP, cl = lane % CGP;
+    constexpr int NG = CG / 4;    // groups of 4 components per chunk
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    // TMA destinations must be 128-byte aligned (128 spare bytes are allocated)
+    T *box = reinterpret_cast<T *>(smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127));
+
+    const int tile = blockIdx.x;
+    const int pbeg = tile_off[tile], pend = tile_off[tile + 1];
+    if (pbeg == pend) return;
     const int K = g.K;
-    const long warps = (long)gridDim.x * (kThreads / 32);
-    for (long s = (long)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); s < n; s += warps) {
-        const T wreg = lane < 3 * P ? rec_w[(size_t)s * WS + lane] : T(0);
-        int sx, sy, sz;
-        unpack_start(rec_start[s], sx, sy, sz);
-        const int idx = rec_idx[s];
-        // this lane's x weights and mesh x coordinates
-        T wx[XI];
-        int gx[XI];
+    const int HYB = g.ty + P - 1, HZB = g.tz + P - 1;
+    const int PS = HZB * HYB * kHX;  // component-plane stride
+    const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
+    const int ox = tix * g.tx, oy = tiy * g.ty, oz = tiz * g.tz;
+    const int hx = min(g.tx, K - ox) + P - 1;
+    const int hy = min(g.ty, K - oy) + P - 1;
+    const int hz = min(g.tz, K - oz) + P - 1;
+    // TMA: halo must not wrap, and the box's innermost start coordinate times the
+    // element size must be a multiple of 16 bytes
+    const bool tma = use_tma && ox + hx <= K && oy + hy <= K && oz + hz <= K &&
+                     ((size_t)ox * sizeof(T)) % 16 == 0;
+    const size_t K2 = (size_t)K * K, K3 = K2 * K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int xs = lane >> 2, cl = lane & 3;
+
+    if (tma && threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    int chunk = 0;
+    for (int c0 = 0; c0 < C; c0 += CG, chunk++) {
+        const int nc = min(CG, C - c0);
+        if (tma) {
+            if (threadIdx.x == 0) {
+                fence_proxy_async();  // order earlier generic reads of the box before the TMA write
+                mbar_expect_tx(&bar, (uint32_t)((size_t)CG * PS * sizeof(T)));
+                tma_load_4d(box, &tmap, ox, oy, oz, c0, &bar);
+            }
+            const bool ok = mbar_wait(&bar, (uint32_t)(chunk & 1));
+            if (!__syncthreads_and(ok)) {  // uniform decision: all threads give up together
+                if (threadIdx.x == 0) atomicExch(err, 1);
+                return;
+            }
+        } else {
+            // rows [c][z][y][0..kHX) of the halo region, wrap-aware
+            const bool vec = (K % VW) == 0 && (ox % VW) == 0;
+            DivMod dnv, dhy, dhz;
+            dnv.init(NV);
+            dhy.init(hy);
+            dhz.init(hz);
+            const int nrow = nc * hz * hy;
+            for (int q = threadIdx.x; q < nrow * NV; q += kThreads) {
+                int v, y, z;
+                const int row = dnv.div(q, v);
+                const int cz = dhy.div(row, y);
+                const int c = dhz.div(cz, z);
+                int gy = oy + y, gz = oz + z;
+                gy -= gy >= K ? K : 0;
+                gz -= gz >= K ? K : 0;
+                const T *src = mesh + (size_t)(c0 + c) * K3 + (size_t)gz * K2 + (size_t)gy * K;
+                T *dst = box + (size_t)c * PS + (z * HYB + y) * kHX + v * VW;
+                const int x0 = ox + v * VW;
+                if (vec) {
+                    *reinterpret_cast<V *>(dst) = __ldg(reinterpret_cast<const V *>(src + x0 % K));
+                } else {
 #pragma unroll
-        for (int k = 0; k < XI; k++) {
-            const int x = xs + k * XS;
-            const T v = __shfl_sync(0xffffffffu, wreg, x < P ? x : P - 1);
-            wx[k] = x < P ? v : T(0);
-            int c = sx + (x < P ? x : 0);
-            gx[k] = c >= K ? c - K : c;
+                    for (int e = 0; e < VW; e++) dst[e] = __ldg(src + (x0 + e) % K);
+                }
+            }
+            __syncthreads();
         }
-        for (int cbase = 0; cbase < C; cbase += CC) {
-            T acc[NS];
+        for (int s = pbeg + warp; s < pend; s += kThreads / 32) {
+            const T wreg = lane < 3 * P ? rec_w[(size_t)s * WS + lane] : T(0);
+            int sx, sy, sz;
+            unpack_start(rec_start[s], sx, sy, sz);
+            const int lx = sx - ox, ly = sy - oy, lz = sz - oz;  // own tile: no wrap
+            const T wxv = __shfl_sync(0xffffffffu, wreg, xs < P ? xs : P - 1);
+            const T wx = xs < P ? wxv : T(0);
+            T wxy[P], wz[P];
 #pragma unroll
-            for (int sl = 0; sl < NS; sl++) acc[sl] = T(0);
+            for (int y = 0; y < P; y++) wxy[y] = wx * __shfl_sync(0xffffffffu, wreg, P + y);
+#pragma unroll
+            for (int z = 0; z < P; z++) wz[z] = __shfl_sync(0xffffffffu, wreg, 2 * P + z);
+            T acc[NG];
+#pragma unroll
+            for (int k = 0; k < NG; k++) acc[k] = T(0);
+            const T *base = box + (size_t)cl * PS + (lz * HYB + ly) * kHX + lx + xs;
 #pragma unroll
             for (int z = 0; z < P; z++) {
-                const T wz = __shfl_sync(0xffffffffu, wreg, 2 * P + z);
-                int gz = sz + z;
-                gz = gz >= K ? gz - K : gz;
+                const T *pz = base + z * HYB * kHX;
 #pragma unroll
                 for (int y = 0; y < P; y++) {
-                    const T wzy = wz * __shfl_sync(0xffffffffu, wreg, P + y);
-                    int gy = sy + y;
-                    gy = gy >= K ? gy - K : gy;
-                    const size_t row = ((size_t)gz * K + gy) * K;
+                    const T w = wz[z] * wxy[y];
 #pragma unroll
-                    for (int k = 0; k < XI; k++) {
-                        const T w = wzy * wx[k];
-                        const T *mp = mesh + (row + gx[k]) * C + cbase + cl;
-#pragma unroll
-                        for (int sl = 0; sl < NS; sl++)
-                            if (cbase + sl * CGP + cl < C) acc[sl] += w * __ldg(mp + sl * CGP);
-                    }
+                    for (int k = 0; k < NG; k++) acc[k] += w * pz[(size_t)k * 4 * PS + y * kHX];
                 }
             }
 #pragma unroll
-            for (int sl = 0; sl < NS; sl++)
+            for (int k = 0; k < NG; k++)
 #pragma unroll
-                for (int o = CGP; o < 32; o <<= 1)
-                    acc[sl] += __shfl_xor_sync(0xffffffffu, acc[sl], o);
+                for (int o = 4; o < 32; o <<= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
             if (xs == 0) {
+                T *out = W + (size_t)rec_idx[s] * C + c0;
 #pragma unroll
-                for (int sl = 0; sl < NS; sl++) {
-                    const int c = cbase + sl * CGP + cl;
-                    if (c < C) {
-                        T *o = W + (size_t)idx * C + c;
-                        *o = accumulate ? *o + acc[sl] : acc[sl];
-                    }
+                for (int k = 0; k < NG; k++) {
+                    const int c = 4 * k + cl;
+                    if (c < nc) out[c] = accumulate ? out[c] + acc[k] : acc[k];
                 }
             }
         }
+        __syncthreads();  // the box is rewritten by the next chunk
     }
 }
 
-template <typename T, int P, int CGP, int NS>
-cudaError_t launch_interp_t(int n, const int *rec_idx, const uint32_t *rec_start,
-                            const T *rec_w, const T *mesh, int C, const MeshGeom &g, T *W,
-                            int accumulate, cudaStream_t s) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long need = ((long)n + (kThreads / 32) - 1) / (kThreads / 32);
-    long cap = (long)sms * 8;
-    int blocks = (int)(need < cap ? need : cap);
-    if (blocks < 1) blocks = 1;
-    k_interp<T, P, CGP, NS><<<blocks, kThreads, 0, s>>>(n, rec_idx, rec_start, rec_w, mesh, C,
-                                                        g, W, accumulate);
+template <typename T, int P, int CG>
+size_t interp_smem(const MeshGeom &g) {
+    return (size_t)CG * (g.tz + P - 1) * (g.ty + P - 1) * kHX * sizeof(T) + 128;
+}
+
+template <typename T, int P, int CG>
+cudaError_t launch_interp_t(const InterpMaps &maps, const int *tile_off, const int *rec_idx,
+                            const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
+                            const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
+    const size_t smem = interp_smem<T, P, CG>(g);
+    auto kern = k_interp<T, P, CG>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const bool use = CG == 4 ? maps.ok4 : maps.ok8;
+    const CUtensorMap &m = CG == 4 ? maps.cg4 : maps.cg8;
+    kern<<<g.ntx * g.nty * g.ntz, kThreads, smem, s>>>(m, use ? 1 : 0, tile_off, rec_idx,
+                                                      rec_start, rec_w, mesh, C, g, W,
+                                                      accumulate, err);
     return cudaGetLastError();
 }
 
 template <typename T, int P>
-cudaError_t dispatch_split(int n, const int *rec_idx, const uint32_t *rec_start,
-                           const T *rec_w, const T *mesh, int C, const MeshGeom &g, T *W,
-                           int accumulate, cudaStream_t s) {
-    CompSplit cs = choose_comp_split(C, 1 << 30);
-#define SPME_INTERP_CASE(CG, N)                                                          \
-    if (cs.cgp == CG && cs.ns == N)                                                      \
-        return launch_interp_t<T, P, CG, N>(n, rec_idx, rec_start, rec_w, mesh, C, g, W, \
-                                            accumulate, s);
-    SPME_INTERP_CASE(4, 1)
-    SPME_INTERP_CASE(8, 1)
-    SPME_INTERP_CASE(16, 1)
-    SPME_INTERP_CASE(4, 3)
-    SPME_INTERP_CASE(8, 3)
-    SPME_INTERP_CASE(16, 3)
-#undef SPME_INTERP_CASE
-    return cudaErrorInvalidValue;
+cudaError_t dispatch_cg(const InterpMaps &maps, const int *tile_off, const int *rec_idx,
+                        const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
+                        const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
+    if (interp_chunk(g, sizeof(T), C) == 8)
+        return launch_interp_t<T, P, 8>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W,
+                                        accumulate, err, s);
+    return launch_interp_t<T, P, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W,
+                                    accumulate, err, s);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+bool encode_box(CUtensorMap *m, const void *mesh, int K, int C, const MeshGeom &g, size_t elem,
+                int CG) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || (K * elem) % 16 != 0 || ((uintptr_t)mesh % 16) != 0) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)K, (cuuint64_t)K, (cuuint64_t)K, (cuuint64_t)C};
+    const cuuint64_t strides[3] = {(cuuint64_t)K * elem, (cuuint64_t)K * K * elem,
+                                   (cuuint64_t)K * K * K * elem};
+    const cuuint32_t box[4] = {(cuuint32_t)kHX, (cuuint32_t)(g.ty + g.p - 1),
+                               (cuuint32_t)(g.tz + g.p - 1), (cuuint32_t)CG};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    if (box[1] > 256 || box[2] > 256) return false;
+    CUresult r = fn(m, elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                    4, const_cast<void *>(mesh), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
 }
 
 }  // namespace
 
+int interp_chunk(const MeshGeom &g, size_t elem, int C) {
+    const size_t plane = (size_t)(g.tz + g.p - 1) * (g.ty + g.p - 1) * kHX * elem;
+    return (C > 4 && 8 * plane + 128 <= 110 * 1024) ? 8 : 4;
+}
+
+size_t interp_smem_bytes(const MeshGeom &g, size_t elem) {
+    return (size_t)4 * (g.tz + g.p - 1) * (g.ty + g.p - 1) * kHX * elem + 128;
+}
+
+bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem) {
+    maps->ok4 = encode_box(&maps->cg4, mesh, g.K, C, g, elem, 4);
+    maps->ok8 = encode_box(&maps->cg8, mesh, g.K, C, g, elem, 8);
+    return maps->ok4;
+}
+
 template <typename T>
-cudaError_t launch_interp(int n, const int *rec_idx, const uint32_t *rec_start,
-                          const T *rec_w, const T *mesh, int C, const MeshGeom &g, T *W,
-                          int accumulate, cudaStream_t s) {
+cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, const int *rec_idx,
+                          const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
+                          const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (g.tx + 7 > kHX || g.tx + g.p - 1 > kHX) return cudaErrorInvalidValue;
     switch (g.p) {
-        case 4: return dispatch_split<T, 4>(n, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, s);
-        case 6: return dispatch_split<T, 6>(n, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, s);
-        case 8: return dispatch_split<T, 8>(n, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, s);
+        case 4: return dispatch_cg<T, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, err, s);
+        case 6: return dispatch_cg<T, 6>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, err, s);
+        case 8: return dispatch_cg<T, 8>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, err, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-template cudaError_t launch_interp<float>(int, const int *, const uint32_t *, const float *,
-                                          const float *, int, const MeshGeom &, float *, int,
-                                          cudaStream_t);
-template cudaError_t launch_interp<double>(int, const int *, const uint32_t *, const double *,
-                                           const double *, int, const MeshGeom &, double *, int,
-                                           cudaStream_t);
+template cudaError_t launch_interp<float>(const InterpMaps &, const int *, int, const int *,
+                                          const uint32_t *, const float *, const float *, int,
+                                          const MeshGeom &, float *, int, int *, cudaStream_t);
+template cudaError_t launch_interp<double>(const InterpMaps &, const int *, int, const int *,
+                                           const uint32_t *, const double *, const double *, int,
+                                           const MeshGeom &, double *, int, int *, cudaStream_t);
 
 }  // namespace spme

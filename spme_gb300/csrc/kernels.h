@@ -1,6 +1,7 @@
 // Host-side launchers for the GB300 SPME-RPY kernels (sm_103a).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -28,43 +29,47 @@ void launch_scatter(const int *key, const int *slot, const int *off, int n, int 
 template <typename T>
 void launch_records(const double *pos, const int *perm, int n, const MeshGeom &g,
                     int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s);
-// Wrapped positions in cell-sorted order.
-void launch_cell_positions(const double *pos, const int *perm, int n, double L,
-                           double4 *cpos, cudaStream_t s);
+// Cell-sorted positions relative to their cell's lower corner (float4 or double4).
+void launch_cell_positions(const double *pos, const int *perm, int n, double L, int nc,
+                           bool fp32, void *cpos, cudaStream_t s);
 
 // ---- spread / interpolate (spread.cu, interp.cu) --------------------------
-struct CompSplit {
-    int cgp;  // lanes per component group within a warp (4, 8 or 16)
-    int ns;   // component groups per CTA (1 or 3)
-};
-// Lane split for C components; max_cc caps components per CTA (shared-memory bound).
-CompSplit choose_comp_split(int C, int max_cc);
-size_t spread_smem_bytes(const MeshGeom &g, size_t elem, CompSplit cs);
-constexpr size_t kSpreadSmemCap = 200 * 1024;
 template <typename T>
 cudaError_t launch_spread(const int *tile_off, const int *rec_idx, const uint32_t *rec_start,
                           const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
                           cudaStream_t s);
+// TMA descriptors of the real mesh [C][K][K][K] for the interpolation halo
+// boxes (4- and 8-component chunks).
+struct InterpMaps {
+    CUtensorMap cg4, cg8;
+    bool ok4 = false, ok8 = false;
+};
+bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem);
+// Components staged per chunk for C components (4 or 8).
+int interp_chunk(const MeshGeom &g, size_t elem, int C);
+// Shared memory the interpolation kernel needs with its narrowest (4-component) staging.
+size_t interp_smem_bytes(const MeshGeom &g, size_t elem);
+// err: device flag set to 1 if a TMA wait timed out.
 template <typename T>
-cudaError_t launch_interp(int n, const int *rec_idx, const uint32_t *rec_start,
-                          const T *rec_w, const T *mesh, int C, const MeshGeom &g, T *W,
-                          int accumulate, cudaStream_t s);
+cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, const int *rec_idx,
+                          const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
+                          const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s);
 
 // ---- k-space influence (influence.cu) -------------------------------------
 // tab[(z*K + y)*Kh + kx] = (S(k)|b|^2 / V, S(k)|b|^2 / (V k^2)), zero at k = 0.
 template <typename T>
 void launch_influence_table(T *tab2, const double *bmod2, int K, double L, double xi,
                             double a, cudaStream_t s);
-// In-place influence on the interleaved half spectrum G[(z*K+y)*Kh+kx][C].
+// In-place influence on the component-major half spectrum G[c][(z*K+y)*Kh+kx].
 template <typename T>
 void launch_influence(T *G, const T *tab2, int K, double L, int R, cudaStream_t s);
 
 // ---- real-space pair sum + self term (realspace.cu) -----------------------
+// cpos: float4 for T = float, double4 for T = double (cell-relative).
 template <typename T>
-cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm,
-                             const double4 *cpos, const T *F, int R, double L, double rc,
-                             double xi, double a, int with_real, int with_self, T *W,
-                             cudaStream_t s);
+cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
+                             const T *F, int R, double L, double rc, double xi, double a,
+                             int with_self, T *W, cudaStream_t s);
 
 // ---- layout conversions (pack.cu) -----------------------------------------
 // W = self_c * F (the self term alone, when no real-space sum is requested)

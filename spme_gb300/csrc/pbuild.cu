@@ -169,16 +169,29 @@ __global__ void k_records(const double *__restrict__ pos, const int *__restrict_
     for (int j = 3 * P; j < WS; j++) out[j] = T(0);
 }
 
+// Positions relative to the lower corner of their real-space cell.
+template <typename G4, typename G>
 __global__ void k_cell_positions(const double *__restrict__ pos, const int *__restrict__ perm,
-                                 int n, double L, double4 *__restrict__ cpos) {
+                                 int n, double L, int nc, G4 *__restrict__ cpos) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     int i = perm[s];
-    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    x -= L * floor(x / L);
-    y -= L * floor(y / L);
-    z -= L * floor(z / L);
-    cpos[s] = make_double4(x, y, z, 0.0);
+    const double h = L / nc;
+    double o[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double x = pos[3 * i + d];
+        x -= L * floor(x / L);
+        int c = (int)(x / L * (double)nc);
+        c = c >= nc ? nc - 1 : c;
+        o[d] = x - c * h;
+    }
+    G4 v;
+    v.x = (G)o[0];
+    v.y = (G)o[1];
+    v.z = (G)o[2];
+    v.w = (G)0;
+    cpos[s] = v;
 }
 
 inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
@@ -222,9 +235,15 @@ void launch_records(const double *pos, const int *perm, int n, const MeshGeom &g
     }
 }
 
-void launch_cell_positions(const double *pos, const int *perm, int n, double L,
-                           double4 *cpos, cudaStream_t s) {
-    if (n > 0) k_cell_positions<<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, cpos);
+void launch_cell_positions(const double *pos, const int *perm, int n, double L, int nc,
+                           bool fp32, void *cpos, cudaStream_t s) {
+    if (n <= 0) return;
+    if (fp32)
+        k_cell_positions<float4, float><<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, nc,
+                                                                    (float4 *)cpos);
+    else
+        k_cell_positions<double4, double><<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, nc,
+                                                                      (double4 *)cpos);
 }
 
 template void launch_records<float>(const double *, const int *, int, const MeshGeom &, int *,

@@ -7,8 +7,8 @@
 //
 // One CTA per cell: the cell's particles (chunks of ICH) against the
 // candidates of the 27 neighbour cells (chunks of JCH).  Phase A evaluates each
-// pair within rc once (distance in FP64 with the minimum image, the scalar
-// functions in T) into per-particle shared-memory lists; phase B applies
+// pair within rc once (displacement from cell-relative coordinates, the
+// scalar functions in T) into per-particle shared-memory lists; phase B applies
 // every listed pair tensor to all right-hand sides, one thread per
 // (particle, right-hand side).  Sums over a candidate chunk run in T and are
 // accumulated across chunks in FP64.
@@ -47,15 +47,27 @@ __device__ __forceinline__ void real_FG(T r, T xi, T a, T &F, T &G) {
     G = g / a;
 }
 
-template <typename T, int ICH, int JCH>
+template <typename G> struct Geo4;
+template <> struct Geo4<float> { using type = float4; };
+template <> struct Geo4<double> { using type = double4; };
+
+__device__ __forceinline__ float d_rint(float x) { return rintf(x); }
+__device__ __forceinline__ double d_rint(double x) { return rint(x); }
+
+// T: pair-function and per-chunk accumulation type; G: pair geometry type.
+// Positions are stored relative to the corner of their cell (cell edge
+// h = L/nc), so the displacement to a candidate in neighbour cell c_i + dc is
+// (o_i - o_j) - dc*h, which is accurate in FP32 for any box size.
+template <typename T, typename G, int ICH, int JCH>
 __global__ void __launch_bounds__(kThreads)
 k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ cell_perm,
-            const double4 *__restrict__ cpos, const T *__restrict__ F, int R, double L,
-            double rc2, T xi, T a, T self_c, int with_real, int with_self, T *__restrict__ W) {
+            const typename Geo4<G>::type *__restrict__ cpos, const T *__restrict__ F, int R,
+            G L, G h, G rc2, T xi, T a, T self_c, int with_self, T *__restrict__ W) {
     __shared__ int nb_beg[27], nb_pre[28], nnb;
-    __shared__ double ipos[ICH][3];
+    __shared__ G nb_shift[27][3];
+    __shared__ G ipos[ICH][3];
     __shared__ int iidx[ICH];
-    __shared__ double jpos[JCH][3];
+    __shared__ G jpos[JCH][3];
     __shared__ int jidx[JCH];
     __shared__ int pcnt[ICH];
     __shared__ T pF[ICH][JCH], pG[ICH][JCH], pR[3][ICH][JCH];
@@ -69,17 +81,15 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
         const int cx = cell % nc, cy = (cell / nc) % nc, cz = cell / (nc * nc);
         const int span = nc >= 3 ? 1 : 0;
         int k = 0, pre = 0;
-        int seen[27];
         for (int dz = -span; dz <= span; dz++)
             for (int dy = -span; dy <= span; dy++)
                 for (int dx = -span; dx <= span; dx++) {
                     int c2 = (pmod(cz + dz, nc) * nc + pmod(cy + dy, nc)) * nc + pmod(cx + dx, nc);
-                    bool dup = false;
-                    for (int q = 0; q < k; q++) dup |= seen[q] == c2;
-                    if (dup) continue;
-                    seen[k] = c2;
                     nb_beg[k] = cell_off[c2];
                     nb_pre[k] = pre;
+                    nb_shift[k][0] = (G)dx * h;
+                    nb_shift[k][1] = (G)dy * h;
+                    nb_shift[k][2] = (G)dz * h;
                     pre += cell_off[c2 + 1] - cell_off[c2];
                     k++;
                 }
@@ -89,13 +99,14 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
     __syncthreads();
     const int ncand = nb_pre[nnb];
     const int ib0 = cell_off[cell], ie = cell_off[cell + 1];
-    const double invL = 1.0 / L;
+    const bool single = nc < 3;
+    const G invL = G(1) / L;
 
     for (int ib = ib0; ib < ie; ib += ICH) {
         const int ni = min(ICH, ie - ib);
         __syncthreads();
         if (tid < ni) {
-            double4 p = cpos[ib + tid];
+            const auto p = cpos[ib + tid];
             ipos[tid][0] = p.x;
             ipos[tid][1] = p.y;
             ipos[tid][2] = p.z;
@@ -107,63 +118,64 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
             const int il = tid / rch, r = rb + tid % rch;
             const bool active = tid < ni * rch;
             double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
-            if (with_real) {
-                for (int jb = 0; jb < ncand; jb += JCH) {
-                    const int nj = min(JCH, ncand - jb);
-                    __syncthreads();
-                    if (tid < nj) {
-                        const int cand = jb + tid;
-                        int k = 0;
-                        while (cand >= nb_pre[k + 1]) k++;
-                        const int js = nb_beg[k] + (cand - nb_pre[k]);
-                        double4 p = cpos[js];
-                        jpos[tid][0] = p.x;
-                        jpos[tid][1] = p.y;
-                        jpos[tid][2] = p.z;
-                        jidx[tid] = cell_perm[js];
+            for (int jb = 0; jb < ncand; jb += JCH) {
+                const int nj = min(JCH, ncand - jb);
+                __syncthreads();
+                if (tid < nj) {
+                    const int cand = jb + tid;
+                    int k = 0;
+                    while (cand >= nb_pre[k + 1]) k++;
+                    const int js = nb_beg[k] + (cand - nb_pre[k]);
+                    const auto p = cpos[js];
+                    // candidate position expressed in the frame of cell i
+                    jpos[tid][0] = p.x + nb_shift[k][0];
+                    jpos[tid][1] = p.y + nb_shift[k][1];
+                    jpos[tid][2] = p.z + nb_shift[k][2];
+                    jidx[tid] = cell_perm[js];
+                }
+                if (tid < ICH) pcnt[tid] = 0;
+                __syncthreads();
+                for (int w = tid; w < ni * nj; w += kThreads) {
+                    const int i2 = w / nj, jl = w - (w / nj) * nj;
+                    if (jidx[jl] == iidx[i2]) continue;
+                    G d0 = ipos[i2][0] - jpos[jl][0];
+                    G d1 = ipos[i2][1] - jpos[jl][1];
+                    G d2 = ipos[i2][2] - jpos[jl][2];
+                    if (single) {
+                        d0 -= L * d_rint(d0 * invL);
+                        d1 -= L * d_rint(d1 * invL);
+                        d2 -= L * d_rint(d2 * invL);
                     }
-                    if (tid < ICH) pcnt[tid] = 0;
-                    __syncthreads();
-                    for (int w = tid; w < ni * nj; w += kThreads) {
-                        const int i2 = w / nj, jl = w - (w / nj) * nj;
-                        if (jidx[jl] == iidx[i2]) continue;
-                        double d0 = ipos[i2][0] - jpos[jl][0];
-                        double d1 = ipos[i2][1] - jpos[jl][1];
-                        double d2 = ipos[i2][2] - jpos[jl][2];
-                        d0 -= L * rint(d0 * invL);
-                        d1 -= L * rint(d1 * invL);
-                        d2 -= L * rint(d2 * invL);
-                        const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
-                        if (r2 >= rc2) continue;
-                        const double rr = sqrt(r2);
-                        T Fv, Gv;
-                        real_FG<T>((T)rr, xi, a, Fv, Gv);
-                        const int slot = atomicAdd(&pcnt[i2], 1);
-                        const double ir = 1.0 / rr;
-                        pF[i2][slot] = Fv;
-                        pG[i2][slot] = Gv;
-                        pR[0][i2][slot] = (T)(d0 * ir);
-                        pR[1][i2][slot] = (T)(d1 * ir);
-                        pR[2][i2][slot] = (T)(d2 * ir);
-                        pJ[i2][slot] = jidx[jl];
+                    const G r2 = d0 * d0 + d1 * d1 + d2 * d2;
+                    if (r2 >= rc2) continue;
+                    const G rr = sqrt(r2);
+                    T Fv, Gv;
+                    real_FG<T>((T)rr, xi, a, Fv, Gv);
+                    const int slot = atomicAdd(&pcnt[i2], 1);
+                    const G ir = G(1) / rr;
+                    pF[i2][slot] = Fv;
+                    pG[i2][slot] = Gv;
+                    pR[0][i2][slot] = (T)(d0 * ir);
+                    pR[1][i2][slot] = (T)(d1 * ir);
+                    pR[2][i2][slot] = (T)(d2 * ir);
+                    pJ[i2][slot] = jidx[jl];
+                }
+                __syncthreads();
+                if (active) {
+                    T s0 = T(0), s1 = T(0), s2 = T(0);
+                    const int np_ = pcnt[il];
+                    for (int k = 0; k < np_; k++) {
+                        const T *fj = F + (size_t)pJ[il][k] * C + 3 * r;
+                        const T f0 = fj[0], f1 = fj[1], f2 = fj[2];
+                        const T rx = pR[0][il][k], ry = pR[1][il][k], rz = pR[2][il][k];
+                        const T Fk = pF[il][k], Gd = pG[il][k] * (rx * f0 + ry * f1 + rz * f2);
+                        s0 += Fk * f0 + Gd * rx;
+                        s1 += Fk * f1 + Gd * ry;
+                        s2 += Fk * f2 + Gd * rz;
                     }
-                    __syncthreads();
-                    if (active) {
-                        T s0 = T(0), s1 = T(0), s2 = T(0);
-                        const int np_ = pcnt[il];
-                        for (int k = 0; k < np_; k++) {
-                            const T *fj = F + (size_t)pJ[il][k] * C + 3 * r;
-                            const T f0 = fj[0], f1 = fj[1], f2 = fj[2];
-                            const T rx = pR[0][il][k], ry = pR[1][il][k], rz = pR[2][il][k];
-                            const T Fk = pF[il][k], Gd = pG[il][k] * (rx * f0 + ry * f1 + rz * f2);
-                            s0 += Fk * f0 + Gd * rx;
-                            s1 += Fk * f1 + Gd * ry;
-                            s2 += Fk * f2 + Gd * rz;
-                        }
-                        acc0 += (double)s0;
-                        acc1 += (double)s1;
-                        acc2 += (double)s2;
-                    }
+                    acc0 += (double)s0;
+                    acc1 += (double)s1;
+                    acc2 += (double)s2;
                 }
             }
             if (active) {
@@ -186,29 +198,29 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
 }  // namespace
 
 template <typename T>
-cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm,
-                             const double4 *cpos, const T *F, int R, double L, double rc,
-                             double xi, double a, int with_real, int with_self, T *W,
-                             cudaStream_t s) {
+cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
+                             const T *F, int R, double L, double rc, double xi, double a,
+                             int with_self, T *W, cudaStream_t s) {
     const double rsp = 0.56418958354775628695;
     const double self_c = (1.0 - 6.0 * xi * a * rsp + 40.0 / 3.0 * xi * xi * xi * a * a * a * rsp) / a;
     const int ncell = nc * nc * nc;
+    const double h = L / nc;
     if (sizeof(T) == 8)
-        k_realspace<T, 16, 64><<<ncell, kThreads, 0, s>>>(nc, cell_off, cell_perm, cpos, F, R, L,
-                                                           rc * rc, (T)xi, (T)a, (T)self_c,
-                                                           with_real, with_self, W);
+        k_realspace<T, double, 16, 64><<<ncell, kThreads, 0, s>>>(
+            nc, cell_off, cell_perm, (const double4 *)cpos, F, R, L, h, rc * rc, (T)xi, (T)a,
+            (T)self_c, with_self, W);
     else
-        k_realspace<T, 16, 96><<<ncell, kThreads, 0, s>>>(nc, cell_off, cell_perm, cpos, F, R, L,
-                                                           rc * rc, (T)xi, (T)a, (T)self_c,
-                                                           with_real, with_self, W);
+        k_realspace<T, float, 16, 96><<<ncell, kThreads, 0, s>>>(
+            nc, cell_off, cell_perm, (const float4 *)cpos, F, R, (float)L, (float)h,
+            (float)(rc * rc), (T)xi, (T)a, (T)self_c, with_self, W);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_realspace<float>(int, const int *, const int *, const double4 *,
+template cudaError_t launch_realspace<float>(int, const int *, const int *, const void *,
                                              const float *, int, double, double, double, double,
-                                             int, int, float *, cudaStream_t);
-template cudaError_t launch_realspace<double>(int, const int *, const int *, const double4 *,
+                                             int, float *, cudaStream_t);
+template cudaError_t launch_realspace<double>(int, const int *, const int *, const void *,
                                               const double *, int, double, double, double,
-                                              double, int, int, double *, cudaStream_t);
+                                              double, int, double *, cudaStream_t);
 
 }  // namespace spme

@@ -77,7 +77,7 @@ def test_recip_fp64_vs_oracle(gpu_lib, case):
     assert relerr(u, ref) < FP64_TOL
 
 
-@pytest.mark.parametrize("tile", [(4, 4, 4), (8, 8, 8), (16, 8, 4), (16, 16, 16)])
+@pytest.mark.parametrize("tile", [(4, 4, 4), (8, 8, 8), (16, 8, 4), (16, 16, 4), (8, 16, 8)])
 def test_tile_shapes(gpu_lib, tile):
     n, L, K, p, xi = 700, 30.0, 40, 6, 0.4
     pos, f = uniform_case(n, L, 3, seed=5)
@@ -87,6 +87,14 @@ def test_tile_shapes(gpu_lib, tile):
     u = eng.apply(f)
     ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
     assert relerr(u, ref) < FP64_TOL
+
+
+def test_tile_too_large_is_rejected(gpu_lib):
+    # FP64, p = 8: a 16x16x8 tile's interpolation halo does not fit shared memory
+    with pytest.raises(spme_gb300.SpmeError) as ei:
+        spme_gb300.Engine(100, 30.0, 0.4, 40, 8, precision="fp64", terms=spme_gb300.TERM_RECIP,
+                          tile=(16, 16, 8))
+    assert ei.value.code == 2
 
 
 @pytest.mark.parametrize("radius", [1.0, 1.5])
