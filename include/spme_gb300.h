@@ -42,7 +42,8 @@ enum {
     SPME_ERR_CUFFT = 4,       /* cuFFT error */
     SPME_ERR_NOMEM = 5,       /* device or host allocation failed */
     SPME_ERR_STATE = 6,       /* e.g. apply before any positions were given */
-    SPME_ERR_KERNEL = 7       /* a device-side check failed (status read back) */
+    SPME_ERR_KERNEL = 7,      /* a device-side check failed (status read back) */
+    SPME_ERR_TOO_LARGE = 8    /* exceeds the fixed scratch of spme_realspace_apply_noalloc */
 };
 
 enum { SPME_FP64 = 0, SPME_FP32 = 1 };
@@ -116,6 +117,28 @@ long spme_launch_count(const spme_t *spme);
  * 4..16, tz in 4..8).  Takes effect at the next spme_set_positions, which must
  * follow before the next apply. */
 int spme_set_tile(spme_t *spme, int tx, int ty, int tz);
+
+/* Real-space + self mobility apply that allocates no device memory.
+ * No counterpart in the reference (which has no real-space term).  For callers
+ * that cannot call cudaMalloc: applications that reserve all device memory in
+ * their own pool at start-up, and time-stepping loops that must not stall
+ * (cudaMalloc/cudaFree can synchronise the device).  FP64, device pointers,
+ * work ordered on `stream` (NULL: the legacy default stream):
+ *   u_r = beta*u_r + alpha * (M_real + M_self) f_r,  layout v[r*ld + 3i + d],
+ * with the same Beenakker real-space sum and self term as spme_apply.
+ * Scratch is one fixed device array inside the library (about 16 MB, held on
+ * every GPU that loads the library until exit), so the sizes are capped:
+ * np <= SPME_NOALLOC_MAX_NP, nrhs <= SPME_NOALLOC_MAX_NRHS; larger requests
+ * return SPME_ERR_TOO_LARGE.  All calls share that array: calls that overlap
+ * on the GPU race and must be serialised by the caller.  The first call on a
+ * device looks up the array's device address; make it before any stream
+ * capture. */
+#define SPME_NOALLOC_MAX_NP 65536
+#define SPME_NOALLOC_MAX_NRHS 4
+int spme_realspace_apply_noalloc(int np, const double *pos, double box_size, double xi,
+                                 double radius, double rcut, int nrhs, double alpha,
+                                 const double *f, long ldf, double beta, double *u, long ldu,
+                                 void *stream);
 
 #ifdef __cplusplus
 }

@@ -663,6 +663,9 @@ const char *spme_error_string(int code) {
         case SPME_ERR_NOMEM: return "out of memory";
         case SPME_ERR_STATE: return "engine state error (positions not set)";
         case SPME_ERR_KERNEL: return "device-side check failed";
+        case SPME_ERR_TOO_LARGE:
+            return "request exceeds the fixed scratch of the allocation-free entry point "
+                   "(np <= SPME_NOALLOC_MAX_NP, nrhs <= SPME_NOALLOC_MAX_NRHS)";
         default: return "unknown error";
     }
 }
