@@ -118,6 +118,26 @@ long spme_launch_count(const spme_t *spme);
  * follow before the next apply. */
 int spme_set_tile(spme_t *spme, int tx, int ty, int tz);
 
+/* Ewald parameters for a target relative error `tol` (host only; the reference
+ * declares cutoff2xi for parameter selection, old-version/spme.h:85-86, but
+ * never defines it).  Error models fitted to the oracle: real space
+ * exp(-x^2)(1 + x^4/3) = tol with x = xi rc; k-space tail exp(-y)(1 + y + 2y^2)
+ * = tol with y = (pi K/L)^2/(4 xi^2); B-spline interpolation xi L/K <=
+ * c_p tol^(1/p); p = 4 / 6 / 8 for tol >= 1e-3 / >= 1e-6 / below; K the next
+ * 2^a 3^b 5^c.  rcut <= 0 picks rc = min(10 a, 0.49 L).  Fills *out, all terms. */
+int spme_suggest_params(int np, double box_size, double radius, double tol, double rcut,
+                        spme_params *out);
+/* Smallest n' >= max(n, 2) whose prime factors are 2, 3 and 5. */
+int spme_next_smooth(int n);
+
+/* Particle files in the reference driver's .xyz format (old-version/main.c:46-127):
+ * '#' comment lines, a header line "np L", then "name x y z a" per particle.
+ * spme_read_xyz wraps positions into [0, L) like the driver does and returns
+ * malloc'd arrays (release with spme_free); radii may be NULL. */
+int spme_read_xyz(const char *path, int *np, double *box_size, double **pos, double **radii);
+int spme_write_xyz(const char *path, int np, double box_size, const double *pos, double radius);
+void spme_free(void *p);
+
 /* Real-space + self mobility apply that allocates no device memory.
  * No counterpart in the reference (which has no real-space term).  For callers
  * that cannot call cudaMalloc: applications that reserve all device memory in

@@ -86,6 +86,12 @@ def load(path: str | None = None):
         "create_spme_engine": (None, [d, i, i, i, d, i, ctypes.POINTER(_P)]),
         "destroy_spme_engine": (None, [_P]),
         "compute_spme": (None, [_P, _P, i, d, _P, i, d, _P, i]),
+        "spme_suggest_params": (i, [i, d, d, d, d, ctypes.POINTER(Params)]),
+        "spme_next_smooth": (i, [i]),
+        "spme_read_xyz": (i, [ctypes.c_char_p, ctypes.POINTER(i), ctypes.POINTER(d),
+                              ctypes.POINTER(ctypes.POINTER(d)), ctypes.POINTER(ctypes.POINTER(d))]),
+        "spme_write_xyz": (i, [ctypes.c_char_p, i, d, _P, d]),
+        "spme_free": (None, [_P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -149,6 +155,42 @@ def compute_spme(h, pos, nrhs: int, alpha: float, vec_in, ldin: int, beta: float
     lib.compute_spme(h, pp.ctypes.data_as(_P) if pp is not None else None, nrhs, alpha,
                      vin.ctypes.data_as(_P), ldin, beta, vec_out.ctypes.data_as(_P), ldout)
     _check(lib.spme_last_error(h), "compute_spme")
+
+
+def suggest_params(np_: int, box_size: float, radius: float = 1.0, tol: float = 1e-5,
+                   rcut: float = 0.0) -> dict:
+    """Ewald parameters (xi, K, p, rc) for a target relative error (host only)."""
+    out = Params()
+    _check(load().spme_suggest_params(int(np_), float(box_size), float(radius), float(tol),
+                                      float(rcut), ctypes.byref(out)), "spme_suggest_params")
+    return {"np": out.np, "box_size": out.box_size, "xi": out.xi, "dim": out.dim,
+            "porder": out.porder, "radius": out.radius, "rcut": out.rcut}
+
+
+def next_smooth(n: int) -> int:
+    return int(load().spme_next_smooth(int(n)))
+
+
+def read_xyz(path: str):
+    """(positions (N,3) wrapped into [0,L), L, radii) from a reference-format .xyz."""
+    lib = load()
+    n, L = ctypes.c_int(), ctypes.c_double()
+    pp, rp = ctypes.POINTER(ctypes.c_double)(), ctypes.POINTER(ctypes.c_double)()
+    _check(lib.spme_read_xyz(path.encode(), ctypes.byref(n), ctypes.byref(L), ctypes.byref(pp),
+                             ctypes.byref(rp)), "spme_read_xyz")
+    try:
+        pos = np.ctypeslib.as_array(pp, shape=(n.value, 3)).copy()
+        rad = np.ctypeslib.as_array(rp, shape=(n.value,)).copy()
+    finally:
+        lib.spme_free(ctypes.cast(pp, _P))
+        lib.spme_free(ctypes.cast(rp, _P))
+    return pos, L.value, rad
+
+
+def write_xyz(path: str, pos, box_size: float, radius: float = 1.0) -> None:
+    pp = np.ascontiguousarray(pos, dtype=np.float64)
+    _check(load().spme_write_xyz(path.encode(), pp.shape[0], float(box_size),
+                                 pp.ctypes.data_as(_P), float(radius)), "spme_write_xyz")
 
 
 # ---------------------------------------------------------------------------
