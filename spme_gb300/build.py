@@ -16,6 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspme_gb300.so")
+DRIVER = os.path.join(HERE, "pme")
+DRIVER_SRC = os.path.join(HERE, "driver", "pme.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -69,7 +71,24 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         tmp = LIB + ".tmp"
         run([nv, *ARCH, "-shared", "-o", tmp, *objs, "-lcufft"])
         os.replace(tmp, LIB)
+    build_driver(verbose)
     return LIB
+
+
+def build_driver(verbose: bool = False) -> str:
+    """The `pme` command-line driver (host C++ over the C ABI, rpath to the library)."""
+    if (os.path.exists(DRIVER) and os.path.getmtime(DRIVER) > os.path.getmtime(DRIVER_SRC)
+            and os.path.getmtime(DRIVER) > os.path.getmtime(LIB)):
+        return DRIVER
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), DRIVER_SRC,
+           "-L" + HERE, "-lspme_gb300", "-Wl,-rpath,$ORIGIN", "-lm", "-o", DRIVER]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":
