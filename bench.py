@@ -279,7 +279,7 @@ def run_gb300(args, w):
     pos_h = torch.tensor(pos).pin_memory().numpy()
     f_h = torch.tensor(f).pin_memory().numpy()
     u_h = torch.zeros(f.shape, dtype=torch.float32).pin_memory().numpy()
-    eng.set_stream(None)
+    eng.set_stream(None)  # the engine's own stream for the host-pointer API
     for _ in range(max(1, args.warmup)):
         eng.set_positions(pos_h)
         eng.apply(f_h, u_h)

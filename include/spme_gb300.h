@@ -80,8 +80,11 @@ int spme_create(const spme_params *params, spme_t **out);
 /* Destroy an engine; NULL is a no-op. */
 int spme_destroy(spme_t *spme);
 
-/* Run subsequent work on `stream` (a cudaStream_t; NULL = the engine's own). */
+/* Run subsequent work on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream).  An engine starts on a non-blocking stream of its own, which
+ * spme_get_stream returns before any spme_set_stream call. */
 int spme_set_stream(spme_t *spme, void *stream);
+void *spme_get_stream(const spme_t *spme);
 
 /* Load positions (np x 3 doubles; host or device per `mem`) and build the
  * B-spline records, the mesh-tile sort and the real-space cell list.
@@ -112,6 +115,14 @@ int spme_stage_times(const spme_t *spme, float *ms, int n);
 /* Number of this library's kernels the engine has launched since creation
  * (cuFFT's own kernels are not included). */
 long spme_launch_count(const spme_t *spme);
+
+/* Capture each mesh pass (and each device-pointer position build) into a CUDA
+ * graph the first time it is seen and replay it afterwards (on = 1).  A pass
+ * is keyed by nrhs, the f/u pointers and leading dimensions, alpha, beta, the
+ * profiling level and the stream; host-pointer calls capture only their
+ * device work (the copies to and from the caller's memory stay outside).
+ * Turning graphs on or off, or changing the tile, drops all graphs. */
+int spme_set_graphs(spme_t *spme, int on);
 
 /* Mesh-tile shape used by spread/interpolate (default 8 x 8 x 8; tx, ty in
  * 4..16, tz in 4..8).  Takes effect at the next spme_set_positions, which must

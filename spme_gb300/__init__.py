@@ -73,6 +73,7 @@ def load(path: str | None = None):
         "spme_create": (i, [ctypes.POINTER(Params), ctypes.POINTER(_P)]),
         "spme_destroy": (i, [_P]),
         "spme_set_stream": (i, [_P, _P]),
+        "spme_get_stream": (_P, [_P]),
         "spme_set_positions": (i, [_P, _P, i]),
         "spme_apply": (i, [_P, i, d, _P, l, d, _P, l, i]),
         "spme_synchronize": (i, [_P]),
@@ -80,6 +81,7 @@ def load(path: str | None = None):
         "spme_stage_times": (i, [_P, ctypes.POINTER(ctypes.c_float), i]),
         "spme_launch_count": (l, [_P]),
         "spme_set_tile": (i, [_P, i, i, i]),
+        "spme_set_graphs": (i, [_P, i]),
         "spme_last_error": (i, [_P]),
         "spme_error_string": (ctypes.c_char_p, [i]),
         "cutoff2xi": (None, [d, d, d, ctypes.POINTER(d)]),
@@ -206,8 +208,9 @@ class Engine:
 
     ``precision`` "fp64" or "fp32"; ``max_nrhs`` right-hand sides go through one
     mesh pass.  Vectors use compute_spme's layout (rows of 3N per right-hand
-    side): numpy arrays (host, copied in the call) or CUDA tensors (device,
-    stream-ordered on the engine's stream).
+    side): numpy arrays (host, copied in the call, which returns when the
+    result is in place) or CUDA tensors (device; the work is ordered on
+    torch's current stream, like any torch operation).
     """
 
     def __init__(self, np_: int, box_size: float, xi: float, dim: int, porder: int,
@@ -226,6 +229,8 @@ class Engine:
         h = _P()
         _check(lib.spme_create(ctypes.byref(p), ctypes.byref(h)), "spme_create")
         self.h = h
+        self._own_stream = lib.spme_get_stream(h)
+        self._stream = self._own_stream
         if tile is not None:
             _check(lib.spme_set_tile(h, *tile), "spme_set_tile")
 
@@ -249,13 +254,26 @@ class Engine:
 
     # -- operations ----------------------------------------------------------
     def set_stream(self, stream_ptr: int | None):
-        _check(load().spme_set_stream(self.h, stream_ptr or None), "spme_set_stream")
+        """Run on the given cudaStream_t handle (0: legacy default stream);
+        None returns to the engine's own stream."""
+        s = self._own_stream if stream_ptr is None else (stream_ptr or None)
+        _check(load().spme_set_stream(self.h, s), "spme_set_stream")
+        self._stream = s
+
+    def _follow_torch(self):
+        """CUDA-tensor calls are ordered with torch's current stream."""
+        import torch
+        cur = torch.cuda.current_stream().cuda_stream or None
+        if cur != self._stream:
+            _check(load().spme_set_stream(self.h, cur), "spme_set_stream")
+            self._stream = cur
 
     def set_positions(self, pos):
         lib = load()
         if _is_torch_cuda(pos):
             import torch
             assert pos.dtype == torch.float64 and pos.is_contiguous()
+            self._follow_torch()
             _check(lib.spme_set_positions(self.h, pos.data_ptr(), MEM_DEVICE), "set_positions")
         else:
             pp = np.ascontiguousarray(pos, dtype=np.float64)
@@ -269,6 +287,7 @@ class Engine:
         lib = load()
         if _is_torch_cuda(f):
             import torch
+            self._follow_torch()
             f2 = f.reshape(-1, 3 * self.np)
             if u is None:
                 u = torch.zeros_like(f2)
@@ -300,6 +319,13 @@ class Engine:
         buf = (ctypes.c_float * len(STAGES))()
         n = load().spme_stage_times(self.h, buf, len(STAGES))
         return {STAGES[k]: float(buf[k]) for k in range(n)}
+
+    def set_graphs(self, on: bool = True):
+        """Replay captured CUDA graphs for repeated passes (see spme_set_graphs)."""
+        _check(load().spme_set_graphs(self.h, 1 if on else 0), "spme_set_graphs")
+
+    def set_tile(self, tx: int, ty: int, tz: int):
+        _check(load().spme_set_tile(self.h, tx, ty, tz), "spme_set_tile")
 
     def launch_count(self) -> int:
         return int(load().spme_launch_count(self.h))

@@ -25,6 +25,20 @@ namespace {
 
 constexpr int kStages = 8;
 
+// One captured pass (or position build) and the key it was captured for.
+struct GraphEntry {
+    bool valid = false;
+    int R = 0, prof = 0;
+    const void *f = nullptr;
+    void *u = nullptr;
+    long ldf = 0, ldu = 0;
+    double alpha = 0.0, beta = 0.0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long launches = 0;
+};
+constexpr int kGraphSlots = 4;
+
 struct PlanPair {
     int C;
     cufftHandle fwd;
@@ -40,6 +54,7 @@ struct _spme_t {
     int device = 0;
     int last_error = SPME_OK;
     cudaStream_t own_stream = nullptr, stream = nullptr, aux = nullptr;
+    cudaStream_t cap_stream = nullptr;  // graph capture when the caller's stream is the legacy default
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int profiling = 0;  // 1: stage events; 2: events + real-space serialized
     cudaEvent_t ev[kStages + 1] = {};
@@ -72,6 +87,12 @@ struct _spme_t {
     void *d_F = nullptr, *d_W = nullptr, *d_fstage = nullptr, *d_ustage = nullptr;
     int *d_err = nullptr;  // device-side error flag (TMA wait timeouts)
     size_t cap_tiles = 0;  // allocated tile-count capacity
+    // CUDA graphs: passes and device-pointer position builds are captured once
+    // per key and replayed (spme_set_graphs)
+    bool use_graphs = false;
+    GraphEntry gpass[kGraphSlots];
+    int gnext = 0;
+    GraphEntry gpos;
 };
 
 namespace {
@@ -282,6 +303,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
     }
     TRY_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
     TRY_CUDA(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking));
+    TRY_CUDA(cudaStreamCreateWithFlags(&e->cap_stream, cudaStreamNonBlocking));
     e->stream = e->own_stream;
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
@@ -336,11 +358,65 @@ int create_impl(const spme_params &prm, spme_t **out) {
     return SPME_OK;
 }
 
+void drop_graph(GraphEntry &g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = GraphEntry();
+}
+
+void drop_graphs(spme_t *e) {
+    for (GraphEntry &g : e->gpass) drop_graph(g);
+    drop_graph(e->gpos);
+    e->gnext = 0;
+}
+
+// Capture `body` on the engine's stream into g (launch count of the captured
+// kernels kept for the replays), then launch it.
+void use_stream(spme_t *e, cudaStream_t s) {
+    e->stream = s;
+    for (PlanPair &p : e->plans) {
+        cufftSetStream(p.fwd, s);
+        cufftSetStream(p.bwd, s);
+    }
+}
+
+template <typename F>
+int capture_and_launch(spme_t *e, GraphEntry &g, F body) {
+    const long l0 = e->launches;
+    // the legacy default stream cannot be captured: capture on a side stream
+    // (ordered after the default stream's earlier work) and launch there
+    const cudaStream_t orig = e->stream;
+    const cudaStream_t cs = orig ? orig : e->cap_stream;
+    if (cs != orig) use_stream(e, cs);
+    TRY_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    int st = body();
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+    if (cs != orig) use_stream(e, orig);
+    if (st != SPME_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return st != SPME_OK ? st : from_cuda(ce);
+    }
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    TRY_CUDA(ce);
+    drop_graph(g);
+    g.exec = exec;
+    g.launches = e->launches - l0;
+    g.valid = true;
+    e->launches = l0;
+    TRY_CUDA(cudaGraphLaunch(g.exec, e->stream));
+    e->launches += g.launches;
+    return SPME_OK;
+}
+
 void destroy_impl(spme_t *e) {
     if (!e) return;
     DeviceGuard dg(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->aux) cudaStreamSynchronize(e->aux);
+    drop_graphs(e);
     for (PlanPair &p : e->plans) {
         cufftDestroy(p.fwd);
         cufftDestroy(p.bwd);
@@ -358,11 +434,12 @@ void destroy_impl(spme_t *e) {
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->aux) cudaStreamDestroy(e->aux);
+    if (e->cap_stream) cudaStreamDestroy(e->cap_stream);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
     delete e;
 }
 
-int set_positions_impl(spme_t *e, const double *pos, int mem) {
+int set_positions_body(spme_t *e, const double *pos, int mem) {
     const int n = e->prm.np;
     cudaStream_t s = e->stream;
     if (n > 0) {
@@ -372,9 +449,7 @@ int set_positions_impl(spme_t *e, const double *pos, int mem) {
                                                       : cudaMemcpyDeviceToDevice,
                                  s));
     }
-    if (e->prm.terms & SPME_TERM_RECIP) {
-        set_geometry(e);
-        TRY(alloc_tiles(e));
+    if (e->prm.terms & SPME_TERM_RECIP) {  // geometry and tile buffers set by the caller
         TRY_CUDA(cudaMemsetAsync(e->d_tcount, 0, sizeof(int) * e->ntiles, s));
         spme::launch_tile_keys(e->d_pos, n, e->g, e->d_key, e->d_tcount, e->d_slot, s);
         spme::launch_scan(e->d_tcount, e->ntiles, e->d_toff, e->d_scan_tmp, s);
@@ -399,6 +474,26 @@ int set_positions_impl(spme_t *e, const double *pos, int mem) {
         e->launches += 6;
     }
     TRY_CUDA(cudaGetLastError());
+    return SPME_OK;
+}
+
+int set_positions_impl(spme_t *e, const double *pos, int mem) {
+    if (e->prm.np > 0 && !pos) return SPME_ERR_INVALID;
+    if (e->prm.terms & SPME_TERM_RECIP) {
+        set_geometry(e);
+        TRY(alloc_tiles(e));
+    }
+    // host positions come from pageable memory: never captured
+    if (!e->use_graphs || mem != SPME_MEM_DEVICE || e->prm.np == 0) {
+        TRY(set_positions_body(e, pos, mem));
+    } else if (e->gpos.valid && e->gpos.f == pos && e->gpos.stream == e->stream) {
+        TRY_CUDA(cudaGraphLaunch(e->gpos.exec, e->stream));
+        e->launches += e->gpos.launches;
+    } else {
+        TRY(capture_and_launch(e, e->gpos, [&]() { return set_positions_body(e, pos, mem); }));
+        e->gpos.f = pos;
+        e->gpos.stream = e->stream;
+    }
     e->have_pos = true;
     return SPME_OK;
 }
@@ -499,6 +594,49 @@ int check_device_error(spme_t *e) {
     return SPME_OK;
 }
 
+int pass_body(spme_t *e, int R, const void *f, long ldf, void *u, long ldu, double alpha,
+              double beta) {
+    if (is_fp32(e))
+        return run_pass<float>(e, R, (const float *)f, ldf, (float *)u, ldu, alpha, beta);
+    return run_pass<double>(e, R, (const double *)f, ldf, (double *)u, ldu, alpha, beta);
+}
+
+// One mesh pass of R right-hand sides, replayed from a CUDA graph when graphs
+// are on (key: R, pointers, leading dimensions, alpha, beta, profiling level,
+// stream).
+int pass(spme_t *e, int R, const void *f, long ldf, void *u, long ldu, double alpha,
+         double beta) {
+    if (!e->use_graphs) return pass_body(e, R, f, ldf, u, ldu, alpha, beta);
+    for (GraphEntry &g : e->gpass) {
+        if (g.valid && g.R == R && g.f == f && g.u == u && g.ldf == ldf && g.ldu == ldu &&
+            g.alpha == alpha && g.beta == beta && g.prof == e->profiling &&
+            g.stream == e->stream) {
+            TRY_CUDA(cudaGraphLaunch(g.exec, e->stream));
+            e->launches += g.launches;
+            e->ran_real = (e->prm.terms & (SPME_TERM_REAL | SPME_TERM_SELF)) != 0;
+            e->stages_valid = e->profiling > 0;
+            return SPME_OK;
+        }
+    }
+    if (e->prm.terms & SPME_TERM_RECIP) {  // plans (and their work area) before capture
+        PlanPair *pp;
+        TRY(get_plans(e, 3 * R, &pp));
+    }
+    GraphEntry &g = e->gpass[e->gnext];
+    e->gnext = (e->gnext + 1) % kGraphSlots;
+    TRY(capture_and_launch(e, g, [&]() { return pass_body(e, R, f, ldf, u, ldu, alpha, beta); }));
+    g.R = R;
+    g.f = f;
+    g.u = u;
+    g.ldf = ldf;
+    g.ldu = ldu;
+    g.alpha = alpha;
+    g.beta = beta;
+    g.prof = e->profiling;
+    g.stream = e->stream;
+    return SPME_OK;
+}
+
 int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, double beta, void *u,
                long ldu, int mem) {
     const int n = e->prm.np;
@@ -518,21 +656,12 @@ int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
             if (beta != 0.0)
                 TRY_CUDA(cudaMemcpy2DAsync(e->d_ustage, row, up, el * ldu, row, R,
                                            cudaMemcpyHostToDevice, e->stream));
-            if (is_fp32(e))
-                st = run_pass<float>(e, R, (const float *)e->d_fstage, 3L * n,
-                                     (float *)e->d_ustage, 3L * n, alpha, beta);
-            else
-                st = run_pass<double>(e, R, (const double *)e->d_fstage, 3L * n,
-                                      (double *)e->d_ustage, 3L * n, alpha, beta);
+            st = pass(e, R, e->d_fstage, 3L * n, e->d_ustage, 3L * n, alpha, beta);
             TRY(st);
             TRY_CUDA(cudaMemcpy2DAsync(up, el * ldu, e->d_ustage, row, row, R,
                                        cudaMemcpyDeviceToHost, e->stream));
         } else {
-            if (is_fp32(e))
-                st = run_pass<float>(e, R, (const float *)fp, ldf, (float *)up, ldu, alpha, beta);
-            else
-                st = run_pass<double>(e, R, (const double *)fp, ldf, (double *)up, ldu, alpha,
-                                      beta);
+            st = pass(e, R, fp, ldf, up, ldu, alpha, beta);
             TRY(st);
         }
     }
@@ -574,14 +703,12 @@ int spme_destroy(spme_t *e) {
     return SPME_OK;
 }
 
+void *spme_get_stream(const spme_t *e) { return e ? (void *)e->stream : nullptr; }
+
 int spme_set_stream(spme_t *e, void *stream) {
     if (!e) return SPME_ERR_INVALID;
     DeviceGuard dg(e->device);
-    e->stream = stream ? (cudaStream_t)stream : e->own_stream;
-    for (PlanPair &p : e->plans) {
-        cufftSetStream(p.fwd, e->stream);
-        cufftSetStream(p.bwd, e->stream);
-    }
+    use_stream(e, (cudaStream_t)stream);
     return e->last_error = SPME_OK;
 }
 
@@ -648,6 +775,16 @@ int spme_set_tile(spme_t *e, int tx, int ty, int tz) {
     e->tile[1] = ty;
     e->tile[2] = tz;
     e->have_pos = false;
+    drop_graphs(e);
+    return e->last_error = SPME_OK;
+}
+
+int spme_set_graphs(spme_t *e, int on) {
+    if (!e) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    drop_graphs(e);
+    e->use_graphs = on != 0;
     return e->last_error = SPME_OK;
 }
 
