@@ -40,6 +40,9 @@ WORKLOADS = {
     "large": dict(N=1_000_000, L=480.0, K=256, p=6, R=16, xi=0.3, rc=10.0, a=1.0),
     "multi_rhs": dict(N=200_000, L=250.0, K=160, p=6, R=16, xi=0.3, rc=10.0, a=1.0),
     "scale_up": dict(N=100_000, L=220.0, K=128, p=6, R=1, xi=0.3, rc=10.0, a=1.0),
+    # 64 systems, N log-uniform in [500, 50000], phi = 0.05, K = next 2^a3^b5^c >= 0.6 L,
+    # p in {4, 6, 8}, R = 4 (one CUDA-graph launch vs a per-system loop)
+    "uneven_batch": dict(count=64, R=4, xi=0.3, rc=10.0, a=1.0),
 }
 
 # DRAM bytes per launch measured with ncu (dram__bytes_read.sum +
@@ -379,6 +382,71 @@ def run_gb300(args, w):
     return 0
 
 
+def run_batch(args, w):
+    """Uneven batch: all systems in one captured graph vs a per-system loop."""
+    import torch
+
+    from spme_gb300.batch import SystemBatch, uneven_systems
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    systems = uneven_systems(count=w["count"], xi=w["xi"], rc=w["rc"], radius=w["a"],
+                             seed=1234 + rank)
+    R = w["R"]
+    rng = np.random.default_rng(77 + rank)
+    pos = [torch.tensor(rng.uniform(0, s["L"], (s["N"], 3)), device="cuda") for s in systems]
+    f = [torch.tensor(rng.standard_normal((R, 3 * s["N"])), dtype=torch.float32, device="cuda")
+         for s in systems]
+    u = [torch.zeros_like(x) for x in f]
+    b = SystemBatch(systems, nrhs=R)
+    b.bind(pos, f, u)
+    units = sum(s["N"] for s in systems) * R
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        b.run_loop()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run_loop()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    loop_ms = e0.elapsed_time(e1) / args.steps
+    b.capture()
+    for _ in range(args.warmup):
+        b.run()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0.record(b._main)
+    for _ in range(args.steps):
+        b.run()
+    e1.record(b._main)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": ms * 1e6 / units, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: positions U[0,L) and forces N(0,1), seeded",
+        "config": {"workload": f"uneven batch of {w['count']} systems, N log-uniform in "
+                               f"[500, 50000], phi=0.05, K=next smooth >= 0.6 L, p in {{4,6,8}}, "
+                               f"R={R}, xi={w['xi']}, rc={w['rc']}",
+                   "systems": len(systems), "particles": units // R,
+                   "l2": "whole batch larger than L2"},
+        "per_system_loop": {"value": loop_ms * 1e6 / units, "unit": UNIT, "ms_per_step": loop_ms},
+        "graph_speedup_vs_loop": loop_ms / ms,
+        "tiles": {f"N{s['N']}_K{s['K']}_p{s['p']}": list(t) for s, t in zip(systems, b.tiles)},
+        "clocks": ck,
+    }
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -392,6 +460,12 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     w = WORKLOADS[args.workload]
+    if args.workload == "uneven_batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the uneven-batch workload is not a reference configuration"}))
+            return 0
+        return run_batch(args, w)
     if args.impl == "reference":
         return run_reference(args, w)
     return run_gb300(args, w)

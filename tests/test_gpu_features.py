@@ -92,3 +92,33 @@ def test_brownian_displacement_statistics(gpu_lib):
     X = np.concatenate(samples)
     cov = X.T @ X / X.shape[0]
     assert relerr(cov, 2 * 0.5 * M) < 0.08  # 4000 samples: ~1/sqrt(4000) statistical error
+
+
+def test_uneven_batch_graph_matches_loop_and_oracle(gpu_lib, tmp_path, monkeypatch):
+    import torch
+    from spme_gb300.batch import SystemBatch, uneven_systems
+    monkeypatch.setenv("SPME_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    systems = uneven_systems(count=6, nmin=500, nmax=3000, seed=9)
+    R = 4
+    rng = np.random.default_rng(0)
+    pos = [rng.uniform(0, s["L"], (s["N"], 3)) for s in systems]
+    f = [rng.standard_normal((R, 3 * s["N"])) for s in systems]
+    b = SystemBatch(systems, nrhs=R)
+    pos_d = [torch.tensor(p, device="cuda") for p in pos]
+    f_d = [torch.tensor(x, dtype=torch.float32, device="cuda") for x in f]
+    u_d = [torch.zeros_like(x) for x in f_d]
+    b.bind(pos_d, f_d, u_d)
+    b.run_loop()
+    torch.cuda.synchronize()
+    loop = [u.cpu().numpy().copy() for u in u_d]
+    for u in u_d:
+        u.zero_()
+    b.run()
+    b.run()  # replay twice
+    torch.cuda.synchronize()
+    for k, s in enumerate(systems):
+        got = u_d[k].cpu().numpy()
+        assert relerr(got, loop[k]) < 1e-6
+        ref = oracle.full(pos[k], s["L"], s["xi"], s["rc"], s["K"], s["p"], f[k], nthreads=4)
+        assert relerr(got, ref) < 1e-5
+    b.close()
