@@ -236,10 +236,17 @@ def run_gb300(args, w):
     torch.cuda.set_stream(stream)
     eng = spme_gb300.Engine(N, w["L"], w["xi"], w["K"], w["p"], radius=w["a"], rcut=w["rc"],
                             precision="fp32", max_nrhs=R, terms=spme_gb300.TERM_ALL)
-    eng.set_stream(stream.cuda_stream)
     pos_d = torch.tensor(pos, device="cuda")
     f_d = torch.tensor(f, device="cuda")
     u_d = torch.zeros_like(f_d)
+    tune = None
+    if not args.no_autotune:
+        # tile shape measured on this device (outside the timed region, not cached)
+        from spme_gb300.autotune import autotune
+        tile, timings = autotune(eng, pos_d, f_d, reps=2, use_cache=False)
+        tune = {"tile": list(tile),
+                "ms_per_candidate": {"x".join(map(str, k)): round(v, 3) for k, v in timings.items()}}
+    eng.set_stream(stream.cuda_stream)
 
     def step():
         eng.set_positions(pos_d)
@@ -374,6 +381,7 @@ def run_gb300(args, w):
         "clocks": ck,
         "gpu_launches": launches,
         "kernels": kern,
+        "autotune": tune,
     }
     line.update(extra)
     print(json.dumps(line), flush=True)
@@ -456,6 +464,7 @@ def main():
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

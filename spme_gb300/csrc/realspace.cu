@@ -5,20 +5,15 @@
 // scalar_recip at old-version/spme.c:43-60), with the RPY overlap form for
 // pairs closer than 2a.
 //
-// One CTA per cell: the cell's particles (chunks of ICH) against the
-// candidates of the 27 neighbour cells (chunks of JCH).  Phase A evaluates each
-// pair within rc once (displacement from cell-relative coordinates, the
-// scalar functions in T) into per-particle shared-memory lists; phase B applies
-// every listed pair tensor to all right-hand sides, one thread per
-// (particle, right-hand side).  Sums over a candidate chunk run in T and are
-// accumulated across chunks in FP64.
+// One CTA per cell of edge >= rc; a warp per particle of the cell against the
+// candidates of the 27 neighbour cells (details at the kernel below).
 #include "kernels.h"
 
 namespace spme {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 64;  // two warps per cell: ~4-5 particles each at typical densities
 
 __device__ __forceinline__ float d_erfc(float x) { return erfcf(x); }
 __device__ __forceinline__ double d_erfc(double x) { return erfc(x); }
@@ -54,37 +49,50 @@ template <> struct Geo4<double> { using type = double4; };
 __device__ __forceinline__ float d_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double d_rint(double x) { return rint(x); }
 
-// T: pair-function and per-chunk accumulation type; G: pair geometry type.
-// Positions are stored relative to the corner of their cell (cell edge
-// h = L/nc), so the displacement to a candidate in neighbour cell c_i + dc is
-// (o_i - o_j) - dc*h, which is accurate in FP32 for any box size.
-template <typename T, typename G, int ICH, int JCH>
+constexpr int kWarps = kThreads / 32;
+constexpr int kCap = 512;  // candidates staged in shared memory per cell
+
+// T: pair-function type; G: pair geometry type.  Positions are stored relative
+// to the corner of their cell (edge h = L/nc), so the displacement to a
+// candidate in neighbour cell c_i + dc is (o_i - o_j) - dc*h, accurate in
+// FP32 for any box size.
+//
+// One CTA per cell.  The candidates of the 27 neighbour cells are staged once
+// in shared memory (positions in the frame of the CTA's cell), then each warp
+// takes one of the cell's particles at a time:
+//   1. lanes test 32 candidates at a time for r < rc and compact the hits
+//      into a per-warp buffer (ballot + popc);
+//   2. every 32 hits, lanes evaluate the 32 pair functions F, G and unit
+//      vectors (all lanes busy);
+//   3. lanes as (pair, right-hand side) apply the batch to the forces:
+//      u_i[r] += F f_j[r] + G rhat (rhat . f_j[r]).
+// Sums over one batch run in T; batches are accumulated in FP64.  No block
+// barrier after the staging.  More than kCap candidates (very dense cells)
+// take a second path that reads candidates straight from global memory.
+template <typename T, typename G>
 __global__ void __launch_bounds__(kThreads)
 k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ cell_perm,
             const typename Geo4<G>::type *__restrict__ cpos, const T *__restrict__ F, int R,
             G L, G h, G rc2, T xi, T a, T self_c, int with_self, T *__restrict__ W) {
     __shared__ int nb_beg[27], nb_pre[28], nnb;
     __shared__ G nb_shift[27][3];
-    __shared__ G ipos[ICH][3];
-    __shared__ int iidx[ICH];
-    __shared__ G jpos[JCH][3];
-    __shared__ int jidx[JCH];
-    __shared__ int pcnt[ICH];
-    __shared__ T pF[ICH][JCH], pG[ICH][JCH], pR[3][ICH][JCH];
-    __shared__ int pJ[ICH][JCH];
+    __shared__ G cx[kCap], cy[kCap], cz[kCap];
+    __shared__ int cj[kCap];
+    __shared__ int hits[kWarps][64];
+    __shared__ T pF[kWarps][32], pG[kWarps][32], pr[kWarps][3][32];
+    __shared__ int pj[kWarps][32];
 
-    constexpr int RCHMAX = kThreads / ICH;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int cell = blockIdx.x;
     const int C = 3 * R;
     if (tid == 0) {
-        const int cx = cell % nc, cy = (cell / nc) % nc, cz = cell / (nc * nc);
+        const int ccx = cell % nc, ccy = (cell / nc) % nc, ccz = cell / (nc * nc);
         const int span = nc >= 3 ? 1 : 0;
         int k = 0, pre = 0;
         for (int dz = -span; dz <= span; dz++)
             for (int dy = -span; dy <= span; dy++)
                 for (int dx = -span; dx <= span; dx++) {
-                    int c2 = (pmod(cz + dz, nc) * nc + pmod(cy + dy, nc)) * nc + pmod(cx + dx, nc);
+                    int c2 = (pmod(ccz + dz, nc) * nc + pmod(ccy + dy, nc)) * nc + pmod(ccx + dx, nc);
                     nb_beg[k] = cell_off[c2];
                     nb_pre[k] = pre;
                     nb_shift[k][0] = (G)dx * h;
@@ -98,98 +106,149 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
     }
     __syncthreads();
     const int ncand = nb_pre[nnb];
-    const int ib0 = cell_off[cell], ie = cell_off[cell + 1];
+    const bool staged = ncand <= kCap;
+    if (staged) {
+        for (int q = tid; q < ncand; q += kThreads) {
+            int k = 0;
+            while (q >= nb_pre[k + 1]) k++;
+            const int js = nb_beg[k] + (q - nb_pre[k]);
+            const auto p = cpos[js];
+            cx[q] = p.x + nb_shift[k][0];
+            cy[q] = p.y + nb_shift[k][1];
+            cz[q] = p.z + nb_shift[k][2];
+            cj[q] = cell_perm[js];
+        }
+    }
+    __syncthreads();
     const bool single = nc < 3;
     const G invL = G(1) / L;
+    const int ib0 = cell_off[cell], ie = cell_off[cell + 1];
 
-    for (int ib = ib0; ib < ie; ib += ICH) {
-        const int ni = min(ICH, ie - ib);
-        __syncthreads();
-        if (tid < ni) {
-            const auto p = cpos[ib + tid];
-            ipos[tid][0] = p.x;
-            ipos[tid][1] = p.y;
-            ipos[tid][2] = p.z;
-            iidx[tid] = cell_perm[ib + tid];
+    // candidate q -> position in this cell's frame and particle id
+    auto candidate = [&](int q, G &x, G &y, G &z, int &j) {
+        if (staged) {
+            x = cx[q];
+            y = cy[q];
+            z = cz[q];
+            j = cj[q];
+        } else {
+            int k = 0;
+            while (q >= nb_pre[k + 1]) k++;
+            const int js = nb_beg[k] + (q - nb_pre[k]);
+            const auto p = cpos[js];
+            x = p.x + nb_shift[k][0];
+            y = p.y + nb_shift[k][1];
+            z = p.z + nb_shift[k][2];
+            j = cell_perm[js];
         }
-        __syncthreads();
-        for (int rb = 0; rb < R; rb += RCHMAX) {
-            const int rch = min(RCHMAX, R - rb);
-            const int il = tid / rch, r = rb + tid % rch;
-            const bool active = tid < ni * rch;
-            double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
-            for (int jb = 0; jb < ncand; jb += JCH) {
-                const int nj = min(JCH, ncand - jb);
-                __syncthreads();
-                if (tid < nj) {
-                    const int cand = jb + tid;
-                    int k = 0;
-                    while (cand >= nb_pre[k + 1]) k++;
-                    const int js = nb_beg[k] + (cand - nb_pre[k]);
-                    const auto p = cpos[js];
-                    // candidate position expressed in the frame of cell i
-                    jpos[tid][0] = p.x + nb_shift[k][0];
-                    jpos[tid][1] = p.y + nb_shift[k][1];
-                    jpos[tid][2] = p.z + nb_shift[k][2];
-                    jidx[tid] = cell_perm[js];
-                }
-                if (tid < ICH) pcnt[tid] = 0;
-                __syncthreads();
-                for (int w = tid; w < ni * nj; w += kThreads) {
-                    const int i2 = w / nj, jl = w - (w / nj) * nj;
-                    if (jidx[jl] == iidx[i2]) continue;
-                    G d0 = ipos[i2][0] - jpos[jl][0];
-                    G d1 = ipos[i2][1] - jpos[jl][1];
-                    G d2 = ipos[i2][2] - jpos[jl][2];
+    };
+
+    const int RL = R >= 32 ? 32 : (R > 16 ? 32 : (R > 8 ? 16 : (R > 4 ? 8 : (R > 2 ? 4 : (R > 1 ? 2 : 1)))));
+    const int PR = 32 / RL;             // pairs applied in parallel
+    const int pp = lane / RL, rl = lane % RL;
+
+    for (int i = ib0 + warp; i < ie; i += kWarps) {
+        const auto pi = cpos[i];
+        const int ii = cell_perm[i];
+        for (int rb = 0; rb < R; rb += RL) {
+            const int r = rb + rl;
+            const bool rok = r < R;
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+            int nh = 0;  // buffered hits (warp-uniform)
+            // evaluate and apply `m` buffered hits; returns this lane's partial sums
+            auto flush = [&](int m, T &s0, T &s1, T &s2) {
+                if (lane < m) {
+                    G x, y, z;
+                    int j;
+                    candidate(hits[warp][lane], x, y, z, j);
+                    G d0 = (G)pi.x - x, d1 = (G)pi.y - y, d2 = (G)pi.z - z;
                     if (single) {
                         d0 -= L * d_rint(d0 * invL);
                         d1 -= L * d_rint(d1 * invL);
                         d2 -= L * d_rint(d2 * invL);
                     }
-                    const G r2 = d0 * d0 + d1 * d1 + d2 * d2;
-                    if (r2 >= rc2) continue;
-                    const G rr = sqrt(r2);
+                    const G rr = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
                     T Fv, Gv;
                     real_FG<T>((T)rr, xi, a, Fv, Gv);
-                    const int slot = atomicAdd(&pcnt[i2], 1);
                     const G ir = G(1) / rr;
-                    pF[i2][slot] = Fv;
-                    pG[i2][slot] = Gv;
-                    pR[0][i2][slot] = (T)(d0 * ir);
-                    pR[1][i2][slot] = (T)(d1 * ir);
-                    pR[2][i2][slot] = (T)(d2 * ir);
-                    pJ[i2][slot] = jidx[jl];
+                    pF[warp][lane] = Fv;
+                    pG[warp][lane] = Gv;
+                    pr[warp][0][lane] = (T)(d0 * ir);
+                    pr[warp][1][lane] = (T)(d1 * ir);
+                    pr[warp][2][lane] = (T)(d2 * ir);
+                    pj[warp][lane] = j;
                 }
-                __syncthreads();
-                if (active) {
-                    T s0 = T(0), s1 = T(0), s2 = T(0);
-                    const int np_ = pcnt[il];
-                    for (int k = 0; k < np_; k++) {
-                        const T *fj = F + (size_t)pJ[il][k] * C + 3 * r;
+                __syncwarp();
+                s0 = s1 = s2 = T(0);
+                if (rok) {
+                    for (int k = pp; k < m; k += PR) {
+                        const T *fj = F + (size_t)pj[warp][k] * C + 3 * r;
                         const T f0 = fj[0], f1 = fj[1], f2 = fj[2];
-                        const T rx = pR[0][il][k], ry = pR[1][il][k], rz = pR[2][il][k];
-                        const T Fk = pF[il][k], Gd = pG[il][k] * (rx * f0 + ry * f1 + rz * f2);
+                        const T rx = pr[warp][0][k], ry = pr[warp][1][k], rz = pr[warp][2][k];
+                        const T Fk = pF[warp][k], Gd = pG[warp][k] * (rx * f0 + ry * f1 + rz * f2);
                         s0 += Fk * f0 + Gd * rx;
                         s1 += Fk * f1 + Gd * ry;
                         s2 += Fk * f2 + Gd * rz;
                     }
-                    acc0 += (double)s0;
-                    acc1 += (double)s1;
-                    acc2 += (double)s2;
+                }
+                __syncwarp();
+            };
+            for (int q0 = 0; q0 < ncand; q0 += 32) {
+                const int q = q0 + lane;
+                bool hit = false;
+                if (q < ncand) {
+                    G x, y, z;
+                    int j;
+                    candidate(q, x, y, z, j);
+                    if (j != ii) {
+                        G d0 = (G)pi.x - x, d1 = (G)pi.y - y, d2 = (G)pi.z - z;
+                        if (single) {
+                            d0 -= L * d_rint(d0 * invL);
+                            d1 -= L * d_rint(d1 * invL);
+                            d2 -= L * d_rint(d2 * invL);
+                        }
+                        hit = d0 * d0 + d1 * d1 + d2 * d2 < rc2;
+                    }
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) hits[warp][nh + __popc(m & ((1u << lane) - 1u))] = q;
+                nh += __popc(m);
+                __syncwarp();
+                if (nh >= 32) {
+                    T s0, s1, s2;
+                    flush(32, s0, s1, s2);
+                    a0 += (double)s0;
+                    a1 += (double)s1;
+                    a2 += (double)s2;
+                    if (lane < nh - 32) hits[warp][lane] = hits[warp][32 + lane];
+                    nh -= 32;
+                    __syncwarp();
                 }
             }
-            if (active) {
-                const int i = iidx[il];
-                const T *fi = F + (size_t)i * C + 3 * r;
+            if (nh > 0) {
+                T s0, s1, s2;
+                flush(nh, s0, s1, s2);
+                a0 += (double)s0;
+                a1 += (double)s1;
+                a2 += (double)s2;
+            }
+            // sum the PR pair slots of each right-hand side
+            for (int o = RL; o < 32; o <<= 1) {
+                a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+                a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+                a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+            }
+            if (pp == 0 && rok) {
+                const T *fi = F + (size_t)ii * C + 3 * r;
                 if (with_self) {
-                    acc0 += (double)self_c * (double)fi[0];
-                    acc1 += (double)self_c * (double)fi[1];
-                    acc2 += (double)self_c * (double)fi[2];
+                    a0 += (double)self_c * (double)fi[0];
+                    a1 += (double)self_c * (double)fi[1];
+                    a2 += (double)self_c * (double)fi[2];
                 }
-                T *o = W + (size_t)i * C + 3 * r;
-                o[0] = (T)acc0;
-                o[1] = (T)acc1;
-                o[2] = (T)acc2;
+                T *o = W + (size_t)ii * C + 3 * r;
+                o[0] = (T)a0;
+                o[1] = (T)a1;
+                o[2] = (T)a2;
             }
         }
     }
@@ -205,12 +264,12 @@ cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, 
     const double self_c = (1.0 - 6.0 * xi * a * rsp + 40.0 / 3.0 * xi * xi * xi * a * a * a * rsp) / a;
     const int ncell = nc * nc * nc;
     const double h = L / nc;
-    if (sizeof(T) == 8)
-        k_realspace<T, double, 16, 64><<<ncell, kThreads, 0, s>>>(
+    if constexpr (sizeof(T) == 8)
+        k_realspace<T, double><<<ncell, kThreads, 0, s>>>(
             nc, cell_off, cell_perm, (const double4 *)cpos, F, R, L, h, rc * rc, (T)xi, (T)a,
             (T)self_c, with_self, W);
     else
-        k_realspace<T, float, 16, 96><<<ncell, kThreads, 0, s>>>(
+        k_realspace<T, float><<<ncell, kThreads, 0, s>>>(
             nc, cell_off, cell_perm, (const float4 *)cpos, F, R, (float)L, (float)h,
             (float)(rc * rc), (T)xi, (T)a, (T)self_c, with_self, W);
     return cudaGetLastError();
