@@ -116,6 +116,14 @@ int spme_stage_times(const spme_t *spme, float *ms, int n);
  * (cuFFT's own kernels are not included). */
 long spme_launch_count(const spme_t *spme);
 
+/* Transform strategy of the mesh pass.  1: cuFFT 2D (y, x) transforms of
+ * every z-plane, then one fused kernel doing the z transform, the influence
+ * and the inverse z transform in shared memory (one pass over the half
+ * spectrum instead of three).  0: cuFFT 3D transforms and a separate
+ * influence kernel.  Default: 1 in FP32 when K fits the fused kernel, else 0.
+ * Mode 1 on an engine whose K does not fit returns SPME_ERR_UNSUPPORTED. */
+int spme_set_fft_mode(spme_t *spme, int mode);
+
 /* Capture each mesh pass (and each device-pointer position build) into a CUDA
  * graph the first time it is seen and replay it afterwards (on = 1).  A pass
  * is keyed by nrhs, the f/u pointers and leading dimensions, alpha, beta, the

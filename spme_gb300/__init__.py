@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libspme_gb300.so")
 
 SPME_OK = 0
+ERR_INVALID, ERR_UNSUPPORTED = 1, 2
 SPME_FP64, SPME_FP32 = 0, 1
 TERM_RECIP, TERM_REAL, TERM_SELF, TERM_ALL = 1, 2, 4, 7
 MEM_HOST, MEM_DEVICE = 0, 1
@@ -82,6 +83,7 @@ def load(path: str | None = None):
         "spme_launch_count": (l, [_P]),
         "spme_set_tile": (i, [_P, i, i, i]),
         "spme_set_graphs": (i, [_P, i]),
+        "spme_set_fft_mode": (i, [_P, i]),
         "spme_last_error": (i, [_P]),
         "spme_error_string": (ctypes.c_char_p, [i]),
         "cutoff2xi": (None, [d, d, d, ctypes.POINTER(d)]),
@@ -323,6 +325,10 @@ class Engine:
     def set_graphs(self, on: bool = True):
         """Replay captured CUDA graphs for repeated passes (see spme_set_graphs)."""
         _check(load().spme_set_graphs(self.h, 1 if on else 0), "spme_set_graphs")
+
+    def set_fft_mode(self, mode: int):
+        """1: 2D cuFFT + fused z-FFT/influence kernel (default); 0: 3D cuFFT + influence."""
+        _check(load().spme_set_fft_mode(self.h, int(mode)), "spme_set_fft_mode")
 
     def set_tile(self, tx: int, ty: int, tz: int):
         _check(load().spme_set_tile(self.h, tx, ty, tz), "spme_set_tile")

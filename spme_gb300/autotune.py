@@ -16,8 +16,8 @@ import json
 import math
 import os
 
-CANDIDATES = [(8, 8, 8), (8, 8, 4), (16, 8, 8), (16, 8, 4), (16, 16, 4), (8, 16, 8),
-              (4, 4, 4), (12, 12, 8)]
+CANDIDATES = [(8, 8, 8), (8, 8, 4), (8, 4, 4), (16, 4, 4), (16, 8, 8), (16, 8, 4),
+              (16, 16, 4), (8, 16, 8), (4, 4, 4), (12, 12, 8)]
 
 
 def cache_path() -> str:

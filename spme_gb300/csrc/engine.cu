@@ -43,6 +43,8 @@ struct PlanPair {
     int C;
     cufftHandle fwd;
     cufftHandle bwd;
+    cufftHandle fwd2 = 0, bwd2 = 0;  // 2D (y, x) transforms of every z-plane
+    bool has2d = false;
     spme::InterpMaps maps;  // TMA boxes over the mesh for this C and tile shape
     int maps_tile[3];
 };
@@ -86,6 +88,12 @@ struct _spme_t {
     std::vector<PlanPair> plans;
     void *d_F = nullptr, *d_W = nullptr, *d_fstage = nullptr, *d_ustage = nullptr;
     int *d_err = nullptr;  // device-side error flag (TMA wait timeouts)
+    // FFT mode 1: 2D cuFFT + fused z-FFT/influence kernel; 0: 3D cuFFT + influence
+    int fft_mode = 1;
+    spme::ZPlan zp{};
+    void *d_ztw = nullptr;
+    int *d_zip = nullptr;
+    CUtensorMap zmap;  // over the half spectrum (fft_mode 1)
     size_t cap_tiles = 0;  // allocated tile-count capacity
     // CUDA graphs: passes and device-pointer position builds are captured once
     // per key and replayed (spme_set_graphs)
@@ -280,6 +288,43 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
     TRY_FFT(cufftSetWorkArea(pp.bwd, e->d_work));
     TRY_FFT(cufftSetStream(pp.fwd, e->stream));
     TRY_FFT(cufftSetStream(pp.bwd, e->stream));
+    if (e->fft_mode == 1) {
+        // 2D (y, x) transforms of the C*K z-planes: same memory layout as the
+        // 3D transform's first two stages
+        const int Khp = K / 2 + 1;
+        int n2[2] = {K, K}, re2[2] = {K, K}, ce2[2] = {K, Khp};
+        size_t w3 = 0, w4 = 0;
+        TRY_FFT(cufftCreate(&pp.fwd2));
+        TRY_FFT(cufftCreate(&pp.bwd2));
+        TRY_FFT(cufftSetAutoAllocation(pp.fwd2, 0));
+        TRY_FFT(cufftSetAutoAllocation(pp.bwd2, 0));
+        const int P2 = K * K, C2 = K * Khp;
+        TRY_FFT(cufftMakePlanMany(pp.fwd2, 2, n2, re2, 1, P2, ce2, 1, C2, tf, C * K, &w3));
+        TRY_FFT(cufftMakePlanMany(pp.bwd2, 2, n2, ce2, 1, C2, re2, 1, P2, tb, C * K, &w4));
+        const size_t ws2d = std::max(w3, w4);
+        if (ws2d > e->work_bytes) {
+            dfree(e->d_work);
+            e->d_work = nullptr;
+            e->work_bytes = 0;
+            TRY(dalloc(&e->d_work, ws2d));
+            e->work_bytes = ws2d;
+            for (PlanPair &q : e->plans) {
+                TRY_FFT(cufftSetWorkArea(q.fwd, e->d_work));
+                TRY_FFT(cufftSetWorkArea(q.bwd, e->d_work));
+                if (q.has2d) {
+                    TRY_FFT(cufftSetWorkArea(q.fwd2, e->d_work));
+                    TRY_FFT(cufftSetWorkArea(q.bwd2, e->d_work));
+                }
+            }
+            TRY_FFT(cufftSetWorkArea(pp.fwd, e->d_work));
+            TRY_FFT(cufftSetWorkArea(pp.bwd, e->d_work));
+        }
+        TRY_FFT(cufftSetWorkArea(pp.fwd2, e->d_work));
+        TRY_FFT(cufftSetWorkArea(pp.bwd2, e->d_work));
+        TRY_FFT(cufftSetStream(pp.fwd2, e->stream));
+        TRY_FFT(cufftSetStream(pp.bwd2, e->stream));
+        pp.has2d = true;
+    }
     e->plans.push_back(pp);
     *out = &e->plans.back();
     return SPME_OK;
@@ -345,6 +390,27 @@ int create_impl(const spme_params &prm, spme_t **out) {
                                                  prm.box_size, prm.xi, prm.radius, e->stream);
         e->launches++;
         TRY_CUDA(cudaGetLastError());
+        std::vector<double> twd;
+        std::vector<int> ip;
+        if (spme::zfft_width((int)K, e->elem) > 0 && spme::make_zplan((int)K, e->elem, &e->zp, &twd, &ip) &&
+            spme::make_zfft_map(&e->zmap, e->d_cmesh, (int)K, (int)C, e->elem)) {
+            TRY(dalloc(&e->d_ztw, 2 * e->elem * K));
+            TRY(dalloc(&e->d_zip, sizeof(int) * K));
+            if (is_fp32(e)) {
+                std::vector<float> twf(twd.begin(), twd.end());
+                TRY_CUDA(cudaMemcpy(e->d_ztw, twf.data(), sizeof(float) * twf.size(),
+                                    cudaMemcpyHostToDevice));
+            } else {
+                TRY_CUDA(cudaMemcpy(e->d_ztw, twd.data(), sizeof(double) * twd.size(),
+                                    cudaMemcpyHostToDevice));
+            }
+            TRY_CUDA(cudaMemcpy(e->d_zip, ip.data(), sizeof(int) * K, cudaMemcpyHostToDevice));
+            // measured on GB300 (K = 256): the fused path wins in FP32; in FP64
+            // the 3D transforms + influence are as fast
+            e->fft_mode = is_fp32(e) ? 1 : 0;
+        } else {
+            e->fft_mode = 0;
+        }
         PlanPair *pp;
         TRY(get_plans(e, (int)C, &pp));
     }
@@ -376,6 +442,10 @@ void use_stream(spme_t *e, cudaStream_t s) {
     for (PlanPair &p : e->plans) {
         cufftSetStream(p.fwd, s);
         cufftSetStream(p.bwd, s);
+        if (p.has2d) {
+            cufftSetStream(p.fwd2, s);
+            cufftSetStream(p.bwd2, s);
+        }
     }
 }
 
@@ -420,12 +490,17 @@ void destroy_impl(spme_t *e) {
     for (PlanPair &p : e->plans) {
         cufftDestroy(p.fwd);
         cufftDestroy(p.bwd);
+        if (p.has2d) {
+            cufftDestroy(p.fwd2);
+            cufftDestroy(p.bwd2);
+        }
     }
     void *bufs[] = {e->d_pos,    e->d_key,     e->d_slot,  e->d_tcount,   e->d_toff,
                     e->d_tperm,  e->d_scan_tmp, e->d_rec_idx, e->d_rec_start, e->d_rec_w,
                     e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_mesh,
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
-                    e->d_W,      e->d_fstage,  e->d_ustage, e->d_err};
+                    e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
+                    e->d_zip};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -542,19 +617,29 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
                                         (const T *)e->d_rec_w, F, C, e->g, (T *)e->d_mesh, s));
         e->launches++;
         if (prof) cudaEventRecord(e->ev[2], s);
+        const bool fused = e->fft_mode == 1 && pp->has2d;
+        cufftHandle fwd = fused ? pp->fwd2 : pp->fwd, bwd = fused ? pp->bwd2 : pp->bwd;
         if (sizeof(T) == 4)
-            TRY_FFT(cufftExecR2C(pp->fwd, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh));
+            TRY_FFT(cufftExecR2C(fwd, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh));
         else
-            TRY_FFT(cufftExecD2Z(pp->fwd, (cufftDoubleReal *)e->d_mesh,
+            TRY_FFT(cufftExecD2Z(fwd, (cufftDoubleReal *)e->d_mesh,
                                  (cufftDoubleComplex *)e->d_cmesh));
         if (prof) cudaEventRecord(e->ev[3], s);
-        spme::launch_influence<T>((T *)e->d_cmesh, (const T *)e->d_tab, K, e->prm.box_size, R, s);
-        e->launches += 2;
+        if (fused) {
+            TRY_CUDA(spme::launch_zfft_influence<T>(e->zmap, (T *)e->d_cmesh, (const T *)e->d_tab,
+                                                    (const T *)e->d_ztw, e->d_zip, e->zp,
+                                                    e->prm.box_size, R, e->d_err, s));
+            e->launches += 2;
+        } else {
+            spme::launch_influence<T>((T *)e->d_cmesh, (const T *)e->d_tab, K, e->prm.box_size,
+                                      R, s);
+            e->launches += 2;
+        }
         if (prof) cudaEventRecord(e->ev[4], s);
         if (sizeof(T) == 4)
-            TRY_FFT(cufftExecC2R(pp->bwd, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh));
+            TRY_FFT(cufftExecC2R(bwd, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh));
         else
-            TRY_FFT(cufftExecZ2D(pp->bwd, (cufftDoubleComplex *)e->d_cmesh,
+            TRY_FFT(cufftExecZ2D(bwd, (cufftDoubleComplex *)e->d_cmesh,
                                  (cufftDoubleReal *)e->d_mesh));
         if (prof) cudaEventRecord(e->ev[5], s);
         if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
@@ -776,6 +861,27 @@ int spme_set_tile(spme_t *e, int tx, int ty, int tz) {
     e->tile[2] = tz;
     e->have_pos = false;
     drop_graphs(e);
+    return e->last_error = SPME_OK;
+}
+
+int spme_set_fft_mode(spme_t *e, int mode) {
+    if (!e || (mode != 0 && mode != 1)) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    if (mode == 1 && !e->d_ztw) return e->last_error = SPME_ERR_UNSUPPORTED;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    drop_graphs(e);
+    if (mode == 1) {
+        for (PlanPair &p : e->plans) {
+            cufftDestroy(p.fwd);
+            cufftDestroy(p.bwd);
+            if (p.has2d) {
+                cufftDestroy(p.fwd2);
+                cufftDestroy(p.bwd2);
+            }
+        }
+        e->plans.clear();  // rebuilt with their 2D companions on the next pass
+    }
+    e->fft_mode = mode;
     return e->last_error = SPME_OK;
 }
 

@@ -6,6 +6,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace spme {
@@ -63,6 +65,32 @@ void launch_influence_table(T *tab2, const double *bmod2, int K, double L, doubl
 // In-place influence on the component-major half spectrum G[c][(z*K+y)*Kh+kx].
 template <typename T>
 void launch_influence(T *G, const T *tab2, int K, double L, int R, cudaStream_t s);
+
+// ---- fused z-FFT + influence + inverse z-FFT (zfft.cu) --------------------
+struct ZPlan {
+    int K;
+    int nst;              // radix stages
+    int rad[12];          // radices, first stage of the inverse (DIT) first
+    int len_before_last;  // product of the first nst-1 radices
+    int npass;            // passes of one or two stages
+    int pcode[12];        // 10 * R1 + R2 (R2 = 1: single stage)
+    int pspan[12];        // span of the pass's first (R1) stage in DIT order
+};
+// Radix plan, twiddles e^{-2 pi i e/K} (re, im pairs) and the digit-reversal
+// permutation (position p holds frequency perm[p]) for length-K transforms.
+bool make_zplan(int K, size_t elem, ZPlan *zp, std::vector<double> *tw, std::vector<int> *perm);
+// Columns per block for K (0 if K does not fit the fused kernel).
+int zfft_width(int K, size_t elem);
+// TMA descriptor over the half spectrum G[C][K][K][K/2+1] (complex of elem-byte
+// reals), z-planes viewed as flat rows.
+bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem);
+// On the half spectrum after 2D (y, x) R2C transforms: FFT along z,
+// influence (table as launch_influence), inverse FFT along z, Hermitian part of
+// the kx = 0 and K/2 planes.  tw: K complex twiddles of type T; perm: K ints.
+template <typename T>
+cudaError_t launch_zfft_influence(const CUtensorMap &map, T *G, const T *tab2, const T *tw,
+                                  const int *perm, const ZPlan &zp, double L, int R, int *err,
+                                  cudaStream_t s);
 
 // ---- real-space pair sum + self term (realspace.cu) -----------------------
 // cpos: float4 for T = float, double4 for T = double (cell-relative).

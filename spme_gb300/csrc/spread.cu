@@ -74,7 +74,7 @@ __device__ void build_segments(const int *tile_off, const MeshGeom &g, const int
 }
 
 template <typename T, int P, int CPT, int TZ>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, (CPT * TZ > 96 ? 1 : 2))
 k_spread(const int *__restrict__ tile_off, const int *__restrict__ rec_idx,
          const uint32_t *__restrict__ rec_start, const T *__restrict__ rec_w,
          const T *__restrict__ F, int C, MeshGeom g, T *__restrict__ mesh) {
@@ -231,6 +231,11 @@ template <typename T, int P, int TZ>
 cudaError_t dispatch_cpt(const int *tile_off, const int *rec_idx, const uint32_t *rec_start,
                          const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
                          cudaStream_t s) {
+    // with at most 4 register planes, 24 components per thread halve the number
+    // of (warp, particle) visits for many right-hand sides
+    if constexpr (TZ <= 4 && sizeof(T) == 4)
+        if (C >= 16)
+            return launch_spread_t<T, P, 24, TZ>(tile_off, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
     if (C <= 3)
         return launch_spread_t<T, P, 3, TZ>(tile_off, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
     if (C <= 6)

@@ -1,0 +1,632 @@
+// Fused z-transform + k-space influence + inverse z-transform.
+//
+// The 3D R2C/C2R transforms of the mesh are split: cuFFT does the 2D (y, x)
+// transforms of every z-plane, and this kernel does, for one ky row and a
+// chunk of W kx columns of all 3R components, the forward FFT along z, the
+// RPY influence g <- S|b|^2 (I - k k^T/k^2) g (the physics of influence.cu,
+// restating old-version/spme_kernel.c:73-228), and the inverse FFT along z,
+// in shared memory: one read and one write of the half spectrum instead of
+// three streaming passes.
+//
+// Data movement: the half spectrum keeps cuFFT's default layout
+// G[c][z][y][K/2+1] (padded rows make cuFFT's 2D transforms slower).  A chunk's
+// z-columns of one component are one TMA box over the z-planes viewed as flat
+// rows of K (K/2+1) complex values; in FP32 a row segment can start 8 bytes off
+// a 16-byte boundary, so the box starts one complex value early when needed and
+// is two complex values wider (the extra columns are never stored).  Two
+// buffers: while a block transforms right-hand side r, the load of r+1 is in
+// flight.  The last inverse pass writes its results straight to G (masked,
+// coalesced stores), so a buffer is free again as soon as that pass is done.
+//
+// FFT along z (length K = 2^a 3^b 5^c): in-place mixed-radix Cooley-Tukey in
+// shared memory, radices 4, 2, 3, 5.  The forward transform is decimation in
+// frequency (natural order in, digit-reversed order out), the influence is
+// applied in the digit-reversed order (position p holds frequency perm[p]),
+// and the inverse is decimation in time (digit-reversed in, natural out), so
+// no permutation pass is needed.  Neither direction scales (the table's 1/V
+// covers it).
+//
+// The reference's Nyquist convention (influence.cu) needs the Hermitian part
+// on the kx = 0 and (even K) kx = K/2 planes: pairing (ky, kz) with
+// (-ky, -kz) before the inverse z-transform equals pairing (ky, z) with
+// (-ky, z) after it, which k_hermitian_xplanes does on those two planes.
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+
+#include "kernels.h"
+#include "tma.cuh"
+
+namespace spme {
+
+namespace {
+
+constexpr int kZThreads = 384;
+constexpr int kZSmemCap = 220 * 1024;
+
+template <typename T>
+struct Cx {
+    T re, im;
+};
+
+template <typename T>
+__device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T>
+__device__ __forceinline__ Cx<T> cadd(Cx<T> a, Cx<T> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename T>
+__device__ __forceinline__ Cx<T> csub(Cx<T> a, Cx<T> b) { return {a.re - b.re, a.im - b.im}; }
+
+// cos and sin of 2 pi m / R for the radix-3 and radix-5 kernels
+template <int R>
+__device__ __forceinline__ double root_cos(int m);
+template <int R>
+__device__ __forceinline__ double root_sin(int m);
+template <>
+__device__ __forceinline__ double root_cos<3>(int m) { return m == 0 ? 1.0 : -0.5; }
+template <>
+__device__ __forceinline__ double root_sin<3>(int m) {
+    return m == 0 ? 0.0 : (m == 1 ? 0.86602540378443865 : -0.86602540378443865);
+}
+// cos(2 pi/5) = (sqrt 5 - 1)/4, cos(4 pi/5) = -(sqrt 5 + 1)/4
+template <>
+__device__ __forceinline__ double root_cos<5>(int m) {
+    return m == 0 ? 1.0 : ((m == 1 || m == 4) ? 0.30901699437494742 : -0.80901699437494742);
+}
+template <>
+__device__ __forceinline__ double root_sin<5>(int m) {
+    return m == 0 ? 0.0
+                  : (m == 1 ? 0.95105651629515357
+                            : (m == 2 ? 0.58778525229247313
+                                      : (m == 3 ? -0.58778525229247313 : -0.95105651629515357)));
+}
+
+// Radix-R DFT of v into o: o[p] = sum_q v[q] w^{pq}, w = e^{-2 pi i/R}
+// (forward) or its conjugate (INV).
+template <typename T, int R, bool INV>
+__device__ __forceinline__ void dft_small(const Cx<T> (&v)[R], Cx<T> (&o)[R]) {
+    if constexpr (R == 1) {
+        o[0] = v[0];
+    } else if constexpr (R == 2) {
+        o[0] = cadd(v[0], v[1]);
+        o[1] = csub(v[0], v[1]);
+    } else if constexpr (R == 4) {
+        const Cx<T> s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+        const Cx<T> s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+        // -i d13 forward, +i d13 inverse
+        const Cx<T> jd = INV ? Cx<T>{-d13.im, d13.re} : Cx<T>{d13.im, -d13.re};
+        o[0] = cadd(s02, s13);
+        o[1] = cadd(d02, jd);
+        o[2] = csub(s02, s13);
+        o[3] = csub(d02, jd);
+    } else {
+#pragma unroll
+        for (int p = 0; p < R; p++) {
+            Cx<T> s = v[0];
+#pragma unroll
+            for (int q = 1; q < R; q++) {
+                const int m = (p * q) % R;
+                const T c = (T)root_cos<R>(m), sn = (T)(INV ? root_sin<R>(m) : -root_sin<R>(m));
+                s.re += v[q].re * c - v[q].im * sn;
+                s.im += v[q].re * sn + v[q].im * c;
+            }
+            o[p] = s;
+        }
+    }
+}
+
+// One pass = two consecutive radix stages (R1 with span L, then R2 with span
+// L R1; R2 = 1 for a single stage) done in registers, over every column of the
+// block.  Column col = (component g, column w) is fixed per thread (kZThreads
+// is a multiple of 3W); the thread walks pass butterflies bi = bi0, bi0 + BS,
+// ...  Element z of column (g, w) lives at buf[(g K + z) W + w].  A radix-R
+// stage with span L (block span L2 = L R) is
+//   DIT (inverse):  t_q = x[b L2 + j + q L] w^{q j};  x[b L2 + j + p L] = sum_q t_q W_R^{pq}
+//   DIF (forward):  x[b L2 + j + q L] = (sum_p x[b L2 + j + p L] W_R^{pq}) w^{q j}
+// with w = e^{-2 pi i / L2} (conjugated for the inverse) read from the K-point
+// table at stride K / L2.  In a pass, element (q1, q2) sits at
+// b L3 + j + q1 L + q2 L R1 (L3 = L R1 R2); the R2 stage sees span L R1 and
+// offset j + q1 L.  DIT runs the R1 stage first, DIF the R2 stage first.
+// Element z of the thread's column is sb[z RS] in shared memory; with GOUT the
+// results go to gb[z GZ] in global memory instead (only where gok).
+template <typename T, int W, int R1, int R2, bool DIF, bool GOUT>
+__device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int RS, Cx<T> *__restrict__ gb,
+                                      size_t GZ, bool gok, int K, int L,
+                                      const Cx<T> *__restrict__ tw, int bi0) {
+    constexpr int BS = kZThreads / (3 * W);
+    const int La = L * R1, L3 = La * R2;
+    const int nb = K / (R1 * R2), ts1 = K / La, ts2 = K / L3;
+    DivMod dl;
+    dl.init(L);
+    for (int bi = bi0; bi < nb; bi += BS) {
+        int j;
+        const int b = dl.div(bi, j);
+        const int z0 = b * L3 + j;
+        Cx<T> *x = sb + (size_t)z0 * RS;
+        Cx<T> v[R2][R1];
+#pragma unroll
+        for (int q2 = 0; q2 < R2; q2++)
+#pragma unroll
+            for (int q1 = 0; q1 < R1; q1++) v[q2][q1] = x[(q1 * L + q2 * La) * RS];
+        if constexpr (!DIF) {
+#pragma unroll
+            for (int q2 = 0; q2 < R2; q2++) {
+                Cx<T> in[R1], out[R1];
+                in[0] = v[q2][0];
+#pragma unroll
+                for (int q1 = 1; q1 < R1; q1++) {
+                    Cx<T> w = tw[q1 * j * ts1];
+                    w.im = -w.im;
+                    in[q1] = cmul(v[q2][q1], w);
+                }
+                dft_small<T, R1, true>(in, out);
+#pragma unroll
+                for (int p1 = 0; p1 < R1; p1++) v[q2][p1] = out[p1];
+            }
+            if constexpr (R2 > 1) {
+#pragma unroll
+                for (int p1 = 0; p1 < R1; p1++) {
+                    Cx<T> in[R2], out[R2];
+                    in[0] = v[0][p1];
+#pragma unroll
+                    for (int q2 = 1; q2 < R2; q2++) {
+                        Cx<T> w = tw[q2 * (j + p1 * L) * ts2];
+                        w.im = -w.im;
+                        in[q2] = cmul(v[q2][p1], w);
+                    }
+                    dft_small<T, R2, true>(in, out);
+#pragma unroll
+                    for (int p2 = 0; p2 < R2; p2++) v[p2][p1] = out[p2];
+                }
+            }
+        } else {
+            if constexpr (R2 > 1) {
+#pragma unroll
+                for (int p1 = 0; p1 < R1; p1++) {
+                    Cx<T> in[R2], out[R2];
+#pragma unroll
+                    for (int q2 = 0; q2 < R2; q2++) in[q2] = v[q2][p1];
+                    dft_small<T, R2, false>(in, out);
+                    v[0][p1] = out[0];
+#pragma unroll
+                    for (int q2 = 1; q2 < R2; q2++)
+                        v[q2][p1] = cmul(out[q2], tw[q2 * (j + p1 * L) * ts2]);
+                }
+            }
+#pragma unroll
+            for (int q2 = 0; q2 < R2; q2++) {
+                Cx<T> in[R1], out[R1];
+#pragma unroll
+                for (int p1 = 0; p1 < R1; p1++) in[p1] = v[q2][p1];
+                dft_small<T, R1, false>(in, out);
+                v[q2][0] = out[0];
+#pragma unroll
+                for (int q1 = 1; q1 < R1; q1++) v[q2][q1] = cmul(out[q1], tw[q1 * j * ts1]);
+            }
+        }
+        if constexpr (GOUT) {
+            if (gok) {
+                Cx<T> *y = gb + (size_t)z0 * GZ;
+#pragma unroll
+                for (int q2 = 0; q2 < R2; q2++)
+#pragma unroll
+                    for (int q1 = 0; q1 < R1; q1++) y[(size_t)(q1 * L + q2 * La) * GZ] = v[q2][q1];
+            }
+        } else {
+#pragma unroll
+            for (int q2 = 0; q2 < R2; q2++)
+#pragma unroll
+                for (int q1 = 0; q1 < R1; q1++) x[(q1 * L + q2 * La) * RS] = v[q2][q1];
+        }
+    }
+}
+
+// Pass codes: 10 * R1 + R2.
+template <typename T, int W, bool DIF, bool GOUT>
+__device__ __forceinline__ void zstage(Cx<T> *sb, int RS, Cx<T> *gb, size_t GZ, bool gok, int K,
+                                       int code, int L, const Cx<T> *tw, int bi0) {
+    switch (code) {
+        case 44: zpass<T, W, 4, 4, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        case 42: zpass<T, W, 4, 2, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        case 43:
+            // radix-12 / radix-20 passes only in FP32 (register pressure in FP64)
+            if constexpr (sizeof(T) == 4) zpass<T, W, 4, 3, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0);
+            break;
+        case 45:
+            if constexpr (sizeof(T) == 4) zpass<T, W, 4, 5, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0);
+            break;
+        case 41: zpass<T, W, 4, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        case 21: zpass<T, W, 2, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        case 31: zpass<T, W, 3, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        default: zpass<T, W, 5, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+    }
+}
+
+// Shared-memory layout (bytes from the 128-aligned base).  TMA boxes land at
+// 128-byte aligned addresses: each component's K x W block starts on a 128-byte
+// boundary (stride gs complex values), and so does every z chunk of zb rows
+// (checked by zcfg_fits).
+// Shared-memory rows hold W columns plus, in FP32, two more (the widened box).
+template <typename T>
+__host__ __device__ constexpr int zrow(int W) { return W + (sizeof(T) == 4 ? 2 : 0); }
+
+template <typename T>
+struct ZSmem {
+    int gs;            // component stride (complex values)
+    size_t buf_bytes;  // one buffer: 3 components
+    size_t tw_off, perm_off, bar_off, total;
+    __host__ __device__ ZSmem(int K, int W) {
+        const size_t comp = ((size_t)K * zrow<T>(W) * sizeof(Cx<T>) + 127) & ~(size_t)127;
+        gs = (int)(comp / sizeof(Cx<T>));
+        buf_bytes = 3 * comp;
+        tw_off = 2 * buf_bytes;
+        perm_off = tw_off + (size_t)K * sizeof(Cx<T>);
+        bar_off = (perm_off + (size_t)K * sizeof(int) + 15) & ~(size_t)15;
+        total = bar_off + 2 * sizeof(uint64_t);
+    }
+};
+
+// Launch configurations, in order of preference: W columns per block, MAXP
+// influence points per thread (table values kept in registers: points
+// p = p0 + i PS, i < MAXP, so K W <= MAXP kZThreads).  One block per SM (the
+// two buffers take most of the shared memory).
+struct ZCfg {
+    int W, maxp;
+};
+constexpr ZCfg kCfg32[] = {{16, 12}, {8, 12}, {4, 12}, {2, 12}};
+constexpr ZCfg kCfg64[] = {{8, 6}, {4, 6}, {2, 6}, {1, 12}};
+
+template <typename T, int W, int MAXP>
+__global__ void __launch_bounds__(kZThreads, 1)
+k_zfft_influence(const __grid_constant__ CUtensorMap gmap, Cx<T> *__restrict__ G,
+                 const T *__restrict__ tab2, const Cx<T> *__restrict__ tw_g,
+                 const int *__restrict__ perm_g, const __grid_constant__ ZPlan zp, T twopi_L,
+                 int R, int zb, int *__restrict__ err) {
+    using V2 = typename Vec2<T>::type;
+    constexpr int NCOL = 3 * W;
+    constexpr int PS = kZThreads / W;  // z stride of a thread's influence points
+    constexpr int RS = zrow<T>(W);     // shared-memory row (complex values)
+    const int K = zp.K;
+    const int Kh = K / 2 + 1;
+    const size_t plane = (size_t)K * Kh;  // z stride of G (complex values)
+    const int ky = blockIdx.x;
+    const int kx0 = blockIdx.y * W;
+    const int nw = min(W, Kh - kx0);
+    const int tid = threadIdx.x;
+    extern __shared__ __align__(128) unsigned char zsm_raw[];
+    // 128-byte aligned base (the launch reserves 128 bytes of slack)
+    unsigned char *zsm = zsm_raw + ((128u - (smem_addr(zsm_raw) & 127u)) & 127u);
+    const ZSmem<T> lay(K, W);
+    const int GS = lay.gs;
+    Cx<T> *const buf0 = reinterpret_cast<Cx<T> *>(zsm);
+    Cx<T> *const buf1 = reinterpret_cast<Cx<T> *>(zsm + lay.buf_bytes);
+    Cx<T> *tw = reinterpret_cast<Cx<T> *>(zsm + lay.tw_off);
+    int *perm = reinterpret_cast<int *>(zsm + lay.perm_off);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(zsm + lay.bar_off);
+    // flat offset of the chunk in its z-plane; FP32 boxes start on a 16-byte boundary
+    const int flat = ky * Kh + kx0;
+    const int o = sizeof(T) == 4 ? (flat & 1) : 0;
+    const uint32_t box_bytes = (uint32_t)(2 * RS * zb * sizeof(T));
+    const int nzc = K / zb;
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    for (int e = tid; e < K; e += kZThreads) {
+        tw[e] = tw_g[e];
+        perm[e] = perm_g[e];
+    }
+    __syncthreads();
+
+    auto issue_load = [&](int r, int b) {
+        mbar_expect_tx(&bar[b], box_bytes * 3 * nzc);
+        Cx<T> *dst = b ? buf1 : buf0;
+        for (int d = 0; d < 3; d++)
+            for (int zc = 0; zc < nzc; zc++)
+                tma_load_3d(dst + (size_t)d * GS + (size_t)zc * zb * RS, &gmap, 2 * (flat - o),
+                            zc * zb, 3 * r + d, &bar[b]);
+    };
+    if (tid == 0) {
+        issue_load(0, 0);
+        if (R > 1) issue_load(1, 1);
+    }
+
+    // influence table of this thread's points, read once for all R
+    const int wi = tid % W, p0 = tid / W;
+    const int kx = kx0 + wi;
+    const T kxv = (T)kx * twopi_L;  // kx <= K/2: non-negative wavenumber
+    const T kyv = (T)(ky <= K / 2 ? ky : ky - K) * twopi_L;
+    T m2r[MAXP], cr[MAXP];
+#pragma unroll
+    for (int i = 0; i < MAXP; i++) {
+        const int p = p0 + i * PS;
+        m2r[i] = T(0);
+        cr[i] = T(0);
+        if (p < K && kx < Kh) {
+            const int kz = perm[p];
+            const V2 mc =
+                reinterpret_cast<const V2 *>(tab2)[((size_t)kz * K + ky) * Kh + kx];
+            m2r[i] = mc.x;
+            cr[i] = mc.y;
+        }
+    }
+
+    static_assert(kZThreads % NCOL == 0, "columns must tile the block");
+    const int col = tid % NCOL, bi0 = tid / NCOL;
+    const int gcol = col / W, wcol = col - gcol * W;
+    const bool gok = wcol < nw;
+
+    // right-hand side r is the (r >> 1)-th load of buffer r & 1
+    int done = 0;  // right-hand sides consumed
+    for (; done < R; done++) {
+        const int r = done, b = r & 1;
+        const bool ok = mbar_wait(&bar[b], (uint32_t)((r >> 1) & 1));
+        if (!__syncthreads_and(ok)) break;
+        Cx<T> *B = b ? buf1 : buf0;
+        Cx<T> *cb = B + (size_t)gcol * GS + o + wcol;
+        // forward DIF, passes from the last down
+        for (int i = zp.npass - 1; i >= 0; i--) {
+            zstage<T, W, true, false>(cb, RS, nullptr, 0, false, K, zp.pcode[i], zp.pspan[i], tw,
+                                      bi0);
+            __syncthreads();
+        }
+        // influence, digit-reversed z order
+#pragma unroll
+        for (int i = 0; i < MAXP; i++) {
+            const int p = p0 + i * PS;
+            if (p < K) {
+                const int kz = perm[p];
+                const T kzv = (T)(kz <= K / 2 ? kz : kz - K) * twopi_L;
+                const T m2 = m2r[i], c = cr[i];
+                const T b0 = m2 - c * kxv * kxv, b1 = -c * kxv * kyv, b2 = -c * kxv * kzv;
+                const T b3 = m2 - c * kyv * kyv, b4 = -c * kyv * kzv, b5 = m2 - c * kzv * kzv;
+                Cx<T> *q0 = B + (size_t)p * RS + o + wi;
+                Cx<T> *q1 = q0 + GS;
+                Cx<T> *q2 = q1 + GS;
+                const Cx<T> g0 = *q0, g1 = *q1, g2 = *q2;
+                *q0 = {b0 * g0.re + b1 * g1.re + b2 * g2.re, b0 * g0.im + b1 * g1.im + b2 * g2.im};
+                *q1 = {b1 * g0.re + b3 * g1.re + b4 * g2.re, b1 * g0.im + b3 * g1.im + b4 * g2.im};
+                *q2 = {b2 * g0.re + b4 * g1.re + b5 * g2.re, b2 * g0.im + b4 * g1.im + b5 * g2.im};
+            }
+        }
+        __syncthreads();
+        // inverse DIT, passes from the first up; the last one writes G
+        for (int i = 0; i < zp.npass - 1; i++) {
+            zstage<T, W, false, false>(cb, RS, nullptr, 0, false, K, zp.pcode[i], zp.pspan[i], tw,
+                                       bi0);
+            __syncthreads();
+        }
+        Cx<T> *gb = G + (size_t)(3 * r + gcol) * plane * K + flat + wcol;
+        zstage<T, W, false, true>(cb, RS, gb, plane, gok, K, zp.pcode[zp.npass - 1],
+                                  zp.pspan[zp.npass - 1], tw, bi0);
+        __syncthreads();  // buffer b fully read
+        if (tid == 0 && r + 2 < R) issue_load(r + 2, b);
+    }
+    if (tid == 0 && done < R) {
+        atomicExch(err, 1);
+        // loads issued but not consumed: right-hand sides done .. min(done + 1, R - 1);
+        // let them land before the block exits
+        for (int r = done; r < R && r <= done + 1; r++)
+            mbar_wait(&bar[r & 1], (uint32_t)((r >> 1) & 1));
+    }
+}
+
+// Hermitian part over (ky, z) <-> (-ky, z) on the kx = 0 and (even K) kx = K/2
+// planes, after the inverse z-transform.
+template <typename T>
+__global__ void k_hermitian_xplanes(Cx<T> *__restrict__ G, int K, int C) {
+    const int Khp = K / 2 + 1;
+    const int Kh = K / 2 + 1;
+    const int nplanes = (K & 1) ? 1 : 2;
+    const size_t total = (size_t)C * nplanes * K * Kh;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const int y = (int)(t % Kh);
+        size_t rest = t / Kh;
+        const int z = (int)(rest % K);
+        rest /= K;
+        const int pl = (int)(rest % nplanes);
+        const size_t c = rest / nplanes;
+        const int x = pl ? K / 2 : 0;
+        const int y2 = (K - y) % K;
+        const size_t zrow = (c * K + z) * K;
+        Cx<T> *a = G + (zrow + y) * Khp + x;
+        if (y == y2) {
+            a->im = T(0);
+            continue;
+        }
+        Cx<T> *bb = G + (zrow + y2) * Khp + x;
+        const Cx<T> oa = *a, ob = *bb;
+        const Cx<T> h = {T(0.5) * (oa.re + ob.re), T(0.5) * (oa.im - ob.im)};
+        *a = h;
+        *bb = {h.re, -h.im};
+    }
+}
+
+}  // namespace
+
+bool make_zplan(int K, size_t elem, ZPlan *zp, std::vector<double> *twr, std::vector<int> *perm) {
+    if (K < 2 || K > 4096) return false;
+    int m = K, n = 0;
+    int rad[16];
+    for (int r : {4, 2, 3, 5})
+        while (m % r == 0 && n < 16) {
+            rad[n++] = r;
+            m /= r;
+        }
+    if (m != 1 || n > 12) return false;
+    zp->K = K;
+    zp->nst = n;
+    int lb = 1;
+    for (int s = 0; s < n; s++) {
+        zp->rad[s] = rad[s];
+        if (s < n - 1) lb *= rad[s];
+    }
+    zp->len_before_last = lb;  // L at the last stage = product of the first n-1 radices
+    // passes: a radix 4 pairs with the radix after it (in FP64 only with 4 or 2)
+    zp->npass = 0;
+    for (int s = 0, span = 1; s < n;) {
+        int r2 = (rad[s] == 4 && s + 1 < n) ? rad[s + 1] : 1;
+        if (elem == 8 && r2 != 4 && r2 != 2) r2 = 1;
+        const int r1 = rad[s];
+        zp->pcode[zp->npass] = 10 * r1 + r2;
+        zp->pspan[zp->npass] = span;
+        zp->npass++;
+        span *= r1 * r2;
+        s += r2 > 1 ? 2 : 1;
+    }
+    // digit reversal: position p holds natural index perm[p] (recursive
+    // decimation by the last radix first)
+    std::vector<int> idx(K), tmp(K);
+    for (int i = 0; i < K; i++) idx[i] = i;
+    struct Rec {
+        static void run(int *a, int len, const int *rs, int nr, int *scratch) {
+            if (len == 1 || nr == 0) return;
+            const int R = rs[nr - 1], sub = len / R;
+            for (int q = 0; q < R; q++)
+                for (int k = 0; k < sub; k++) scratch[q * sub + k] = a[k * R + q];
+            for (int i = 0; i < len; i++) a[i] = scratch[i];
+            for (int q = 0; q < R; q++) run(a + q * sub, sub, rs, nr - 1, scratch + q * sub);
+        }
+    };
+    Rec::run(idx.data(), K, rad, n, tmp.data());
+    perm->assign(idx.begin(), idx.end());
+    twr->resize(2 * (size_t)K);
+    for (int e = 0; e < K; e++) {
+        const double a = -2.0 * M_PI * (double)e / (double)K;
+        (*twr)[2 * e] = std::cos(a);
+        (*twr)[2 * e + 1] = std::sin(a);
+    }
+    return true;
+}
+
+namespace {
+
+template <typename T>
+size_t zsmem_bytes(int K, int W) {
+    return ZSmem<T>(K, W).total + 128;
+}
+
+int zchunk(int K) {
+    int zb = K;
+    while (zb > 256) zb /= 2;  // TMA box dimensions are at most 256
+    return zb;
+}
+
+bool zcfg_fits(const ZCfg &c, int K, size_t elem) {
+    if ((size_t)2 * c.W * elem % 16 != 0) return false;  // TMA inner box bytes
+    const int zb = zchunk(K);
+    if (K % zb != 0) return false;
+    const int rs = c.W + (elem == 4 ? 2 : 0);
+    if (zb < K && ((size_t)zb * rs * 2 * elem) % 128 != 0) return false;  // chunk alignment
+    if (((size_t)K * (K / 2 + 1) * 2 * elem) % 16 != 0) return false;    // z-plane stride
+    if (kZThreads % (3 * c.W) != 0) return false;
+    const size_t smem = elem == 4 ? zsmem_bytes<float>(K, c.W) : zsmem_bytes<double>(K, c.W);
+    if (smem > (size_t)kZSmemCap) return false;
+    return (size_t)K * c.W <= (size_t)c.maxp * kZThreads;
+}
+
+// Preferred configuration index for K, -1 if none fits.
+int zcfg_index(int K, size_t elem) {
+    const ZCfg *list = elem == 4 ? kCfg32 : kCfg64;
+    const int n = elem == 4 ? (int)(sizeof(kCfg32) / sizeof(ZCfg)) : (int)(sizeof(kCfg64) / sizeof(ZCfg));
+    int first = -1;
+    for (int i = 0; i < n; i++)
+        if (zcfg_fits(list[i], K, elem)) {
+            first = i;
+            break;
+        }
+    const char *ov = getenv("SPME_ZFFT_CFG");
+    if (ov && first >= 0) {
+        const int i = atoi(ov);
+        if (i >= 0 && i < n && zcfg_fits(list[i], K, elem)) return i;
+    }
+    return first;
+}
+
+}  // namespace
+
+int zfft_width(int K, size_t elem) {
+    const int i = zcfg_index(K, elem);
+    if (i < 0) return 0;
+    return (elem == 4 ? kCfg32 : kCfg64)[i].W;
+}
+
+bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem) {
+    EncodeTiledFn fn = encode_fn();
+    const int W = zfft_width(K, elem);
+    if (!fn || W == 0 || ((uintptr_t)G % 16) != 0) return false;
+    const int zb = zchunk(K);
+    const int rs = W + (elem == 4 ? 2 : 0);
+    const cuuint64_t plane = (cuuint64_t)K * (K / 2 + 1) * 2;  // values per z-plane
+    const cuuint64_t dims[3] = {plane, (cuuint64_t)K, (cuuint64_t)C};
+    const cuuint64_t strides[2] = {plane * elem, plane * K * elem};
+    const cuuint32_t box[3] = {(cuuint32_t)(2 * rs), (cuuint32_t)zb, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                    3, G, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+template <typename T, int W, int MAXP>
+cudaError_t launch_zcfg(const CUtensorMap &map, T *G, const T *tab2, const T *tw, const int *perm,
+                        const ZPlan &zp, T twopi_L, int R, int zb, int *err, cudaStream_t s) {
+    auto kern = k_zfft_influence<T, W, MAXP>;
+    const int K = zp.K, Kh = K / 2 + 1;
+    const size_t smem = zsmem_bytes<T>(K, W);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(K, (Kh + W - 1) / W);
+    kern<<<grid, kZThreads, smem, s>>>(map, reinterpret_cast<Cx<T> *>(G), tab2,
+                                       reinterpret_cast<const Cx<T> *>(tw), perm, zp, twopi_L, R,
+                                       zb, err);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_zfft_influence(const CUtensorMap &map, T *G, const T *tab2, const T *tw,
+                                  const int *perm, const ZPlan &zp, double L, int R, int *err,
+                                  cudaStream_t s) {
+    const int K = zp.K, Kh = K / 2 + 1;
+    const int ci = zcfg_index(K, sizeof(T));
+    if (ci < 0) return cudaErrorInvalidValue;
+    const T twopi_L = (T)(2.0 * M_PI / L);
+    const int zb = zchunk(K);
+    cudaError_t e = cudaErrorInvalidValue;
+    const ZCfg c = (sizeof(T) == 4 ? kCfg32 : kCfg64)[ci];
+#define SPME_ZCFG(WW, PP)                                                                       \
+    if (c.W == WW && c.maxp == PP)                                                              \
+        e = launch_zcfg<T, WW, PP>(map, G, tab2, tw, perm, zp, twopi_L, R, zb, err, s);
+    if constexpr (sizeof(T) == 4) {
+        SPME_ZCFG(16, 12)
+        SPME_ZCFG(8, 12)
+        SPME_ZCFG(4, 12)
+        SPME_ZCFG(2, 12)
+    } else {
+        SPME_ZCFG(8, 6)
+        SPME_ZCFG(4, 6)
+        SPME_ZCFG(2, 6)
+        SPME_ZCFG(1, 12)
+    }
+#undef SPME_ZCFG
+    if (e != cudaSuccess) return e;
+    const int nplanes = (K & 1) ? 1 : 2;
+    const size_t work = (size_t)3 * R * nplanes * K * Kh;
+    const int blocks = (int)std::min<size_t>((work + 255) / 256, 152 * 8);
+    k_hermitian_xplanes<T><<<blocks, 256, 0, s>>>(reinterpret_cast<Cx<T> *>(G), K, 3 * R);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_zfft_influence<float>(const CUtensorMap &, float *, const float *,
+                                                  const float *, const int *, const ZPlan &,
+                                                  double, int, int *, cudaStream_t);
+template cudaError_t launch_zfft_influence<double>(const CUtensorMap &, double *, const double *,
+                                                   const double *, const int *, const ZPlan &,
+                                                   double, int, int *, cudaStream_t);
+
+}  // namespace spme

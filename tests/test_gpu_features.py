@@ -122,3 +122,51 @@ def test_uneven_batch_graph_matches_loop_and_oracle(gpu_lib, tmp_path, monkeypat
         ref = oracle.full(pos[k], s["L"], s["xi"], s["rc"], s["K"], s["p"], f[k], nthreads=4)
         assert relerr(got, ref) < 1e-5
     b.close()
+
+
+# (K, p, precision, nrhs): even / odd / 5-smooth K, Nyquist planes, R not a
+# multiple of anything
+FFT_MODE_CASES = [
+    (32, 6, "fp64", 3), (25, 4, "fp64", 2), (45, 8, "fp64", 1), (60, 6, "fp32", 5),
+    (27, 6, "fp32", 4), (128, 6, "fp64", 2), (8, 4, "fp64", 2),
+]
+
+
+@pytest.mark.parametrize("case", FFT_MODE_CASES)
+def test_fused_zfft_matches_3d_fft(gpu_lib, case):
+    """The fused z-FFT/influence kernel against cuFFT 3D + the influence
+    kernel, and both against the oracle."""
+    K, p, prec, R = case
+    n, L, xi = 600, 1.1 * K, 0.35
+    pos, f = uniform_case(n, L, R, seed=K + p)
+    out = {}
+    for mode in (0, 1):
+        eng = spme_gb300.Engine(n, L, xi, K, p, precision=prec, max_nrhs=R,
+                                terms=spme_gb300.TERM_RECIP)
+        eng.set_fft_mode(mode)
+        eng.set_positions(pos)
+        out[mode] = eng.apply(f.astype(eng.dtype))
+        eng.close()
+    ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
+    tol = 1e-12 if prec == "fp64" else 1e-5
+    assert relerr(out[1], ref) < tol
+    assert relerr(out[0], ref) < tol
+    assert relerr(out[1], out[0]) < (1e-13 if prec == "fp64" else 2e-6)
+
+
+def test_fused_mode_unavailable_for_unaligned_fp32_planes(gpu_lib):
+    """FP32 K = 25: a z-plane of the half spectrum is 25 x 13 complex values, not
+    a multiple of 16 bytes, so the fused kernel's TMA boxes cannot address it:
+    mode 1 is refused and the default (3D) path still matches the oracle."""
+    K, p, n, L, xi = 25, 4, 300, 30.0, 0.4
+    pos, f = uniform_case(n, L, 2, seed=3)
+    eng = spme_gb300.Engine(n, L, xi, K, p, precision="fp32", max_nrhs=2,
+                            terms=spme_gb300.TERM_RECIP)
+    with pytest.raises(spme_gb300.SpmeError) as ei:
+        eng.set_fft_mode(1)
+    assert ei.value.code == spme_gb300.ERR_UNSUPPORTED
+    eng.set_positions(pos)
+    u = eng.apply(f.astype(np.float32))
+    ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
+    assert relerr(u, ref) < 1e-5
+    eng.close()
