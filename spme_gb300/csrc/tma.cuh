@@ -62,14 +62,20 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
-// 4D tiled TMA store of one box from shared memory (bulk async-group).  The
-// writing threads must have run fence_proxy_async() and synchronised first.
-__device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, int c0, int c1, int c2,
-                                             int c3, const void *src) {
+// Plain arrival (no transaction bytes) on an mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// 3D tiled TMA store of one box from shared memory (bulk async-group).  The
+// writing threads must have run fence_proxy_async() before the issuing thread
+// learns (through a barrier) that they are done.
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, int c0, int c1, int c2,
+                                             const void *src) {
     asm volatile(
-        "cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::
-            "l"(reinterpret_cast<uint64_t>(map)),
-        "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src))
+        "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+            reinterpret_cast<uint64_t>(map)),
+        "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(src))
         : "memory");
 }
 

@@ -1,22 +1,22 @@
 // Fused z-transform + k-space influence + inverse z-transform.
 //
 // The 3D R2C/C2R transforms of the mesh are split: cuFFT does the 2D (y, x)
-// transforms of every z-plane, and this kernel does, for one ky row and a
-// chunk of W kx columns of all 3R components, the forward FFT along z, the
-// RPY influence g <- S|b|^2 (I - k k^T/k^2) g (the physics of influence.cu,
-// restating old-version/spme_kernel.c:73-228), and the inverse FFT along z,
-// in shared memory: one read and one write of the half spectrum instead of
-// three streaming passes.
+// transforms of every z-plane, and this kernel does, for a chunk of W (y, x)
+// columns of all 3R components, the forward FFT along z, the RPY influence
+// g <- S|b|^2 (I - k k^T/k^2) g (the physics of influence.cu, restating
+// old-version/spme_kernel.c:73-228), and the inverse FFT along z, in shared
+// memory: one read and one write of the half spectrum instead of three
+// streaming passes.
 //
 // Data movement: the half spectrum keeps cuFFT's default layout
-// G[c][z][y][K/2+1] (padded rows make cuFFT's 2D transforms slower).  A chunk's
-// z-columns of one component are one TMA box over the z-planes viewed as flat
-// rows of K (K/2+1) complex values; in FP32 a row segment can start 8 bytes off
-// a 16-byte boundary, so the box starts one complex value early when needed and
-// is two complex values wider (the extra columns are never stored).  Two
-// buffers: while a block transforms right-hand side r, the load of r+1 is in
-// flight.  The last inverse pass writes its results straight to G (masked,
-// coalesced stores), so a buffer is free again as soon as that pass is done.
+// G[c][z][y][K/2+1] (padded rows make cuFFT's 2D transforms slower).  A z-plane
+// is viewed as one flat row of K (K/2+1) columns and cut into chunks of W
+// consecutive columns, so every chunk starts on a 16-byte boundary and its
+// z-columns of one component are one exact TMA box {2W values, zb rows}, for
+// loads and stores alike (columns of two y rows may share a chunk: the
+// transforms are per column).  Two buffers per block; a dedicated warp issues
+// the TMA loads and, once the compute warps hand a buffer back, its TMA store
+// and the load of the next right-hand side into it.
 //
 // FFT along z (length K = 2^a 3^b 5^c): in-place mixed-radix Cooley-Tukey in
 // shared memory, radices 4, 2, 3, 5.  The forward transform is decimation in
@@ -30,8 +30,8 @@
 // on the kx = 0 and (even K) kx = K/2 planes: pairing (ky, kz) with
 // (-ky, -kz) before the inverse z-transform equals pairing (ky, z) with
 // (-ky, z) after it, which k_hermitian_xplanes does on those two planes.
+#include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <vector>
 
 #include "kernels.h"
@@ -41,8 +41,7 @@ namespace spme {
 
 namespace {
 
-constexpr int kZThreads = 384;
-constexpr int kZSmemCap = 220 * 1024;
+constexpr int kZSmemCap = 224 * 1024;
 
 template <typename T>
 struct Cx {
@@ -118,47 +117,48 @@ __device__ __forceinline__ void dft_small(const Cx<T> (&v)[R], Cx<T> (&o)[R]) {
 
 // One pass = two consecutive radix stages (R1 with span L, then R2 with span
 // L R1; R2 = 1 for a single stage) done in registers, over every column of the
-// block.  Column col = (component g, column w) is fixed per thread (kZThreads
-// is a multiple of 3W); the thread walks pass butterflies bi = bi0, bi0 + BS,
-// ...  Element z of column (g, w) lives at buf[(g K + z) W + w].  A radix-R
-// stage with span L (block span L2 = L R) is
+// block.  Column col = (component g, column w) is fixed per thread (the CT
+// compute threads are a multiple of 3W); the thread walks pass butterflies bi = bi0, bi0 + BS,
+// ...  Element z of the thread's column is sb[z W].  A radix-R stage with span
+// L (block span L2 = L R) is
 //   DIT (inverse):  t_q = x[b L2 + j + q L] w^{q j};  x[b L2 + j + p L] = sum_q t_q W_R^{pq}
 //   DIF (forward):  x[b L2 + j + q L] = (sum_p x[b L2 + j + p L] W_R^{pq}) w^{q j}
 // with w = e^{-2 pi i / L2} (conjugated for the inverse) read from the K-point
 // table at stride K / L2.  In a pass, element (q1, q2) sits at
 // b L3 + j + q1 L + q2 L R1 (L3 = L R1 R2); the R2 stage sees span L R1 and
-// offset j + q1 L.  DIT runs the R1 stage first, DIF the R2 stage first.
-// Element z of the thread's column is sb[z RS] in shared memory; with GOUT the
-// results go to gb[z GZ] in global memory instead (only where gok).
-template <typename T, int W, int R1, int R2, bool DIF, bool GOUT>
-__device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int RS, Cx<T> *__restrict__ gb,
-                                      size_t GZ, bool gok, int K, int L,
+// offset j + q1 L.  DIT runs the R1 stage first, DIF the R2 stage first.  A
+// pass with L = 1 has j = 0: its R1-stage twiddles are 1 and are skipped.
+template <typename T, int W, int CT, int R1, int R2, bool DIF>
+__device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int K, int L,
                                       const Cx<T> *__restrict__ tw, int bi0) {
-    constexpr int BS = kZThreads / (3 * W);
+    constexpr int BS = CT / (3 * W);
     const int La = L * R1, L3 = La * R2;
     const int nb = K / (R1 * R2), ts1 = K / La, ts2 = K / L3;
+    const bool unit1 = L == 1;
     DivMod dl;
     dl.init(L);
     for (int bi = bi0; bi < nb; bi += BS) {
         int j;
         const int b = dl.div(bi, j);
-        const int z0 = b * L3 + j;
-        Cx<T> *x = sb + (size_t)z0 * RS;
+        Cx<T> *x = sb + (size_t)(b * L3 + j) * W;
         Cx<T> v[R2][R1];
 #pragma unroll
         for (int q2 = 0; q2 < R2; q2++)
 #pragma unroll
-            for (int q1 = 0; q1 < R1; q1++) v[q2][q1] = x[(q1 * L + q2 * La) * RS];
+            for (int q1 = 0; q1 < R1; q1++) v[q2][q1] = x[(q1 * L + q2 * La) * W];
         if constexpr (!DIF) {
 #pragma unroll
             for (int q2 = 0; q2 < R2; q2++) {
                 Cx<T> in[R1], out[R1];
-                in[0] = v[q2][0];
 #pragma unroll
-                for (int q1 = 1; q1 < R1; q1++) {
-                    Cx<T> w = tw[q1 * j * ts1];
-                    w.im = -w.im;
-                    in[q1] = cmul(v[q2][q1], w);
+                for (int q1 = 0; q1 < R1; q1++) in[q1] = v[q2][q1];
+                if (!unit1) {
+#pragma unroll
+                    for (int q1 = 1; q1 < R1; q1++) {
+                        Cx<T> w = tw[q1 * j * ts1];
+                        w.im = -w.im;
+                        in[q1] = cmul(in[q1], w);
+                    }
                 }
                 dft_small<T, R1, true>(in, out);
 #pragma unroll
@@ -200,99 +200,113 @@ __device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int RS, Cx<T> *__r
 #pragma unroll
                 for (int p1 = 0; p1 < R1; p1++) in[p1] = v[q2][p1];
                 dft_small<T, R1, false>(in, out);
-                v[q2][0] = out[0];
 #pragma unroll
-                for (int q1 = 1; q1 < R1; q1++) v[q2][q1] = cmul(out[q1], tw[q1 * j * ts1]);
+                for (int q1 = 0; q1 < R1; q1++) v[q2][q1] = out[q1];
+                if (!unit1) {
+#pragma unroll
+                    for (int q1 = 1; q1 < R1; q1++) v[q2][q1] = cmul(out[q1], tw[q1 * j * ts1]);
+                }
             }
         }
-        if constexpr (GOUT) {
-            if (gok) {
-                Cx<T> *y = gb + (size_t)z0 * GZ;
 #pragma unroll
-                for (int q2 = 0; q2 < R2; q2++)
+        for (int q2 = 0; q2 < R2; q2++)
 #pragma unroll
-                    for (int q1 = 0; q1 < R1; q1++) y[(size_t)(q1 * L + q2 * La) * GZ] = v[q2][q1];
-            }
-        } else {
-#pragma unroll
-            for (int q2 = 0; q2 < R2; q2++)
-#pragma unroll
-                for (int q1 = 0; q1 < R1; q1++) x[(q1 * L + q2 * La) * RS] = v[q2][q1];
-        }
+            for (int q1 = 0; q1 < R1; q1++) x[(q1 * L + q2 * La) * W] = v[q2][q1];
     }
 }
 
 // Pass codes: 10 * R1 + R2.
-template <typename T, int W, bool DIF, bool GOUT>
-__device__ __forceinline__ void zstage(Cx<T> *sb, int RS, Cx<T> *gb, size_t GZ, bool gok, int K,
-                                       int code, int L, const Cx<T> *tw, int bi0) {
+template <typename T, int W, int CT, bool DIF>
+__device__ __forceinline__ void zstage(Cx<T> *sb, int K, int code, int L, const Cx<T> *tw,
+                                       int bi0) {
     switch (code) {
-        case 44: zpass<T, W, 4, 4, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
-        case 42: zpass<T, W, 4, 2, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        case 44: zpass<T, W, CT, 4, 4, DIF>(sb, K, L, tw, bi0); break;
+        case 42: zpass<T, W, CT, 4, 2, DIF>(sb, K, L, tw, bi0); break;
         case 43:
             // radix-12 / radix-20 passes only in FP32 (register pressure in FP64)
-            if constexpr (sizeof(T) == 4) zpass<T, W, 4, 3, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0);
+            if constexpr (sizeof(T) == 4) zpass<T, W, CT, 4, 3, DIF>(sb, K, L, tw, bi0);
             break;
         case 45:
-            if constexpr (sizeof(T) == 4) zpass<T, W, 4, 5, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0);
+            if constexpr (sizeof(T) == 4) zpass<T, W, CT, 4, 5, DIF>(sb, K, L, tw, bi0);
             break;
-        case 41: zpass<T, W, 4, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
-        case 21: zpass<T, W, 2, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
-        case 31: zpass<T, W, 3, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
-        default: zpass<T, W, 5, 1, DIF, GOUT>(sb, RS, gb, GZ, gok, K, L, tw, bi0); break;
+        case 41: zpass<T, W, CT, 4, 1, DIF>(sb, K, L, tw, bi0); break;
+        case 21: zpass<T, W, CT, 2, 1, DIF>(sb, K, L, tw, bi0); break;
+        case 31: zpass<T, W, CT, 3, 1, DIF>(sb, K, L, tw, bi0); break;
+        default: zpass<T, W, CT, 5, 1, DIF>(sb, K, L, tw, bi0); break;
     }
+}
+
+// Barrier over the CT compute threads only (named barrier 1; the TMA warp
+// never joins it), optionally AND-reducing a predicate.
+template <int CT>
+__device__ __forceinline__ void compute_sync() {
+    asm volatile("bar.sync 1, %0;" ::"n"(CT) : "memory");
+}
+template <int CT>
+__device__ __forceinline__ bool compute_sync_and(bool p) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred q, o;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.and.pred o, 1, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, o;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)p), "n"(CT)
+        : "memory");
+    return r != 0;
 }
 
 // Shared-memory layout (bytes from the 128-aligned base).  TMA boxes land at
 // 128-byte aligned addresses: each component's K x W block starts on a 128-byte
 // boundary (stride gs complex values), and so does every z chunk of zb rows
-// (checked by zcfg_fits).
-// Shared-memory rows hold W columns plus, in FP32, two more (the widened box).
-template <typename T>
-__host__ __device__ constexpr int zrow(int W) { return W + (sizeof(T) == 4 ? 2 : 0); }
-
+// (checked by zcfg_fits).  Barriers: full[b] (TMA load of buffer b landed),
+// done[b] (the compute warps finished buffer b).
 template <typename T>
 struct ZSmem {
     int gs;            // component stride (complex values)
     size_t buf_bytes;  // one buffer: 3 components
     size_t tw_off, perm_off, bar_off, total;
     __host__ __device__ ZSmem(int K, int W) {
-        const size_t comp = ((size_t)K * zrow<T>(W) * sizeof(Cx<T>) + 127) & ~(size_t)127;
+        const size_t comp = ((size_t)K * W * sizeof(Cx<T>) + 127) & ~(size_t)127;
         gs = (int)(comp / sizeof(Cx<T>));
         buf_bytes = 3 * comp;
         tw_off = 2 * buf_bytes;
         perm_off = tw_off + (size_t)K * sizeof(Cx<T>);
         bar_off = (perm_off + (size_t)K * sizeof(int) + 15) & ~(size_t)15;
-        total = bar_off + 2 * sizeof(uint64_t);
+        total = bar_off + 4 * sizeof(uint64_t);
     }
 };
 
-// Launch configurations, in order of preference: W columns per block, MAXP
-// influence points per thread (table values kept in registers: points
-// p = p0 + i PS, i < MAXP, so K W <= MAXP kZThreads).  One block per SM (the
-// two buffers take most of the shared memory).
+// Launch configurations, in order of preference: W columns per block, CT
+// compute threads, MINB blocks per SM, MAXP influence points per thread
+// (table values kept in registers: points p = p0 + i PS, i < MAXP, so
+// K W <= MAXP CT).
 struct ZCfg {
-    int W, maxp;
+    int W, ct, minb, maxp;
 };
-constexpr ZCfg kCfg32[] = {{16, 12}, {8, 12}, {4, 12}, {2, 12}};
-constexpr ZCfg kCfg64[] = {{8, 6}, {4, 6}, {2, 6}, {1, 12}};
+constexpr ZCfg kCfg32[] = {{16, 384, 1, 12}, {8, 192, 2, 12}, {16, 192, 1, 24},
+                           {4, 192, 1, 24},  {2, 192, 1, 24}};
+constexpr ZCfg kCfg64[] = {{8, 384, 1, 6}, {4, 192, 2, 12}, {8, 192, 1, 12},
+                           {2, 192, 1, 24}, {1, 192, 1, 24}};
 
-template <typename T, int W, int MAXP>
-__global__ void __launch_bounds__(kZThreads, 1)
-k_zfft_influence(const __grid_constant__ CUtensorMap gmap, Cx<T> *__restrict__ G,
-                 const T *__restrict__ tab2, const Cx<T> *__restrict__ tw_g,
-                 const int *__restrict__ perm_g, const __grid_constant__ ZPlan zp, T twopi_L,
-                 int R, int zb, int *__restrict__ err) {
+// One block per chunk of W consecutive (y, x) columns of the flattened z-plane
+// (chunk starts are multiples of W: 16-byte aligned in the global layout), all
+// 3R components.  Threads 0..CT-1 transform; the warp after them moves data: TMA loads into
+// the two buffers, TMA stores of finished buffers.
+template <typename T, int W, int CT, int MINB, int MAXP>
+__global__ void __launch_bounds__(CT + 32, MINB)
+k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__ tab2,
+                 const Cx<T> *__restrict__ tw_g, const int *__restrict__ perm_g,
+                 const __grid_constant__ ZPlan zp, T twopi_L, int R, int zb,
+                 int *__restrict__ err) {
     using V2 = typename Vec2<T>::type;
     constexpr int NCOL = 3 * W;
-    constexpr int PS = kZThreads / W;  // z stride of a thread's influence points
-    constexpr int RS = zrow<T>(W);     // shared-memory row (complex values)
+    constexpr int PS = CT / W;  // z stride of a thread's influence points
+    constexpr int NT = CT + 32;
     const int K = zp.K;
     const int Kh = K / 2 + 1;
-    const size_t plane = (size_t)K * Kh;  // z stride of G (complex values)
-    const int ky = blockIdx.x;
-    const int kx0 = blockIdx.y * W;
-    const int nw = min(W, Kh - kx0);
+    const int plane = K * Kh;       // columns per z-plane
+    const int f0 = blockIdx.x * W;  // first flat column of the chunk
     const int tid = threadIdx.x;
     extern __shared__ __align__(128) unsigned char zsm_raw[];
     // 128-byte aligned base (the launch reserves 128 bytes of slack)
@@ -303,40 +317,69 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, Cx<T> *__restrict__ G
     Cx<T> *const buf1 = reinterpret_cast<Cx<T> *>(zsm + lay.buf_bytes);
     Cx<T> *tw = reinterpret_cast<Cx<T> *>(zsm + lay.tw_off);
     int *perm = reinterpret_cast<int *>(zsm + lay.perm_off);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(zsm + lay.bar_off);
-    // flat offset of the chunk in its z-plane; FP32 boxes start on a 16-byte boundary
-    const int flat = ky * Kh + kx0;
-    const int o = sizeof(T) == 4 ? (flat & 1) : 0;
-    const uint32_t box_bytes = (uint32_t)(2 * RS * zb * sizeof(T));
+    uint64_t *full = reinterpret_cast<uint64_t *>(zsm + lay.bar_off);
+    uint64_t *done = full + 2;
     const int nzc = K / zb;
 
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&done[0], CT);
+        mbar_init(&done[1], CT);
         mbar_fence_init();
     }
-    for (int e = tid; e < K; e += kZThreads) {
+    for (int e = tid; e < K; e += NT) {
         tw[e] = tw_g[e];
         perm[e] = perm_g[e];
     }
     __syncthreads();
 
-    auto issue_load = [&](int r, int b) {
-        mbar_expect_tx(&bar[b], box_bytes * 3 * nzc);
-        Cx<T> *dst = b ? buf1 : buf0;
-        for (int d = 0; d < 3; d++)
-            for (int zc = 0; zc < nzc; zc++)
-                tma_load_3d(dst + (size_t)d * GS + (size_t)zc * zb * RS, &gmap, 2 * (flat - o),
-                            zc * zb, 3 * r + d, &bar[b]);
-    };
-    if (tid == 0) {
+    if (tid >= CT) {
+        // ---- TMA warp (one lane) ----
+        if (tid != CT) return;
+        const uint32_t bytes = (uint32_t)(3 * nzc * 2 * W * zb * sizeof(T));
+        auto issue_load = [&](int r, int b) {
+            mbar_expect_tx(&full[b], bytes);
+            Cx<T> *dst = b ? buf1 : buf0;
+            for (int d = 0; d < 3; d++)
+                for (int zc = 0; zc < nzc; zc++)
+                    tma_load_3d(dst + (size_t)d * GS + (size_t)zc * zb * W, &gmap, 2 * f0,
+                                zc * zb, 3 * r + d, &full[b]);
+        };
         issue_load(0, 0);
-        if (R > 1) issue_load(1, 1);
+        int issued = 1;
+        if (R > 1) issue_load(1, 1), issued = 2;
+        int r = 0;
+        for (; r < R; r++) {
+            const int b = r & 1;
+            if (!mbar_wait(&done[b], (uint32_t)((r >> 1) & 1))) break;
+            const Cx<T> *src = b ? buf1 : buf0;
+            for (int d = 0; d < 3; d++)
+                for (int zc = 0; zc < nzc; zc++)
+                    tma_store_3d(&gmap, 2 * f0, zc * zb, 3 * r + d,
+                                 src + (size_t)d * GS + (size_t)zc * zb * W);
+            bulk_commit_group();
+            if (r + 2 < R) {
+                bulk_wait_read_all();  // buffer b is free again
+                issue_load(r + 2, b);
+                issued++;
+            }
+        }
+        if (r < R) {
+            atomicExch(err, 1);
+            // loads of right-hand sides r .. issued-1 may still be in flight
+            for (int q = r; q < issued; q++) mbar_wait(&full[q & 1], (uint32_t)((q >> 1) & 1));
+        }
+        bulk_wait_all();
+        return;
     }
 
+    // ---- compute warps ----
     // influence table of this thread's points, read once for all R
     const int wi = tid % W, p0 = tid / W;
-    const int kx = kx0 + wi;
+    const int fl = f0 + wi;
+    const bool valid = fl < plane;
+    const int ky = valid ? fl / Kh : 0, kx = valid ? fl - ky * Kh : 0;
     const T kxv = (T)kx * twopi_L;  // kx <= K/2: non-negative wavenumber
     const T kyv = (T)(ky <= K / 2 ? ky : ky - K) * twopi_L;
     T m2r[MAXP], cr[MAXP];
@@ -345,33 +388,30 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, Cx<T> *__restrict__ G
         const int p = p0 + i * PS;
         m2r[i] = T(0);
         cr[i] = T(0);
-        if (p < K && kx < Kh) {
-            const int kz = perm[p];
-            const V2 mc =
-                reinterpret_cast<const V2 *>(tab2)[((size_t)kz * K + ky) * Kh + kx];
+        if (p < K && valid) {
+            const V2 mc = reinterpret_cast<const V2 *>(tab2)[(size_t)perm[p] * plane + fl];
             m2r[i] = mc.x;
             cr[i] = mc.y;
         }
     }
 
-    static_assert(kZThreads % NCOL == 0, "columns must tile the block");
+    static_assert(CT % NCOL == 0 && CT % 32 == 0, "columns must tile the compute warps");
     const int col = tid % NCOL, bi0 = tid / NCOL;
     const int gcol = col / W, wcol = col - gcol * W;
-    const bool gok = wcol < nw;
 
-    // right-hand side r is the (r >> 1)-th load of buffer r & 1
-    int done = 0;  // right-hand sides consumed
-    for (; done < R; done++) {
-        const int r = done, b = r & 1;
-        const bool ok = mbar_wait(&bar[b], (uint32_t)((r >> 1) & 1));
-        if (!__syncthreads_and(ok)) break;
+    for (int r = 0; r < R; r++) {
+        const int b = r & 1;
+        const bool ok = mbar_wait(&full[b], (uint32_t)((r >> 1) & 1));
+        if (!compute_sync_and<CT>(ok)) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
         Cx<T> *B = b ? buf1 : buf0;
-        Cx<T> *cb = B + (size_t)gcol * GS + o + wcol;
+        Cx<T> *cb = B + (size_t)gcol * GS + wcol;
         // forward DIF, passes from the last down
         for (int i = zp.npass - 1; i >= 0; i--) {
-            zstage<T, W, true, false>(cb, RS, nullptr, 0, false, K, zp.pcode[i], zp.pspan[i], tw,
-                                      bi0);
-            __syncthreads();
+            zstage<T, W, CT, true>(cb, K, zp.pcode[i], zp.pspan[i], tw, bi0);
+            compute_sync<CT>();
         }
         // influence, digit-reversed z order
 #pragma unroll
@@ -383,7 +423,7 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, Cx<T> *__restrict__ G
                 const T m2 = m2r[i], c = cr[i];
                 const T b0 = m2 - c * kxv * kxv, b1 = -c * kxv * kyv, b2 = -c * kxv * kzv;
                 const T b3 = m2 - c * kyv * kyv, b4 = -c * kyv * kzv, b5 = m2 - c * kzv * kzv;
-                Cx<T> *q0 = B + (size_t)p * RS + o + wi;
+                Cx<T> *q0 = B + (size_t)p * W + wi;
                 Cx<T> *q1 = q0 + GS;
                 Cx<T> *q2 = q1 + GS;
                 const Cx<T> g0 = *q0, g1 = *q1, g2 = *q2;
@@ -392,25 +432,15 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, Cx<T> *__restrict__ G
                 *q2 = {b2 * g0.re + b4 * g1.re + b5 * g2.re, b2 * g0.im + b4 * g1.im + b5 * g2.im};
             }
         }
-        __syncthreads();
-        // inverse DIT, passes from the first up; the last one writes G
-        for (int i = 0; i < zp.npass - 1; i++) {
-            zstage<T, W, false, false>(cb, RS, nullptr, 0, false, K, zp.pcode[i], zp.pspan[i], tw,
-                                       bi0);
-            __syncthreads();
+        compute_sync<CT>();
+        // inverse DIT, passes from the first up
+        for (int i = 0; i < zp.npass; i++) {
+            zstage<T, W, CT, false>(cb, K, zp.pcode[i], zp.pspan[i], tw, bi0);
+            if (i + 1 < zp.npass) compute_sync<CT>();
         }
-        Cx<T> *gb = G + (size_t)(3 * r + gcol) * plane * K + flat + wcol;
-        zstage<T, W, false, true>(cb, RS, gb, plane, gok, K, zp.pcode[zp.npass - 1],
-                                  zp.pspan[zp.npass - 1], tw, bi0);
-        __syncthreads();  // buffer b fully read
-        if (tid == 0 && r + 2 < R) issue_load(r + 2, b);
-    }
-    if (tid == 0 && done < R) {
-        atomicExch(err, 1);
-        // loads issued but not consumed: right-hand sides done .. min(done + 1, R - 1);
-        // let them land before the block exits
-        for (int r = done; r < R && r <= done + 1; r++)
-            mbar_wait(&bar[r & 1], (uint32_t)((r >> 1) & 1));
+        // hand the buffer to the TMA warp (its store reads what this thread wrote)
+        fence_proxy_async();
+        mbar_arrive(&done[b]);
     }
 }
 
@@ -520,31 +550,21 @@ bool zcfg_fits(const ZCfg &c, int K, size_t elem) {
     if ((size_t)2 * c.W * elem % 16 != 0) return false;  // TMA inner box bytes
     const int zb = zchunk(K);
     if (K % zb != 0) return false;
-    const int rs = c.W + (elem == 4 ? 2 : 0);
-    if (zb < K && ((size_t)zb * rs * 2 * elem) % 128 != 0) return false;  // chunk alignment
-    if (((size_t)K * (K / 2 + 1) * 2 * elem) % 16 != 0) return false;    // z-plane stride
-    if (kZThreads % (3 * c.W) != 0) return false;
+    if (zb < K && ((size_t)zb * c.W * 2 * elem) % 128 != 0) return false;  // chunk alignment
+    if (((size_t)K * (K / 2 + 1) * 2 * elem) % 16 != 0) return false;     // z-plane stride
+    if (c.ct % (3 * c.W) != 0) return false;
     const size_t smem = elem == 4 ? zsmem_bytes<float>(K, c.W) : zsmem_bytes<double>(K, c.W);
-    if (smem > (size_t)kZSmemCap) return false;
-    return (size_t)K * c.W <= (size_t)c.maxp * kZThreads;
+    if (smem * c.minb > (size_t)kZSmemCap) return false;
+    return (size_t)K * c.W <= (size_t)c.maxp * c.ct;
 }
 
 // Preferred configuration index for K, -1 if none fits.
 int zcfg_index(int K, size_t elem) {
     const ZCfg *list = elem == 4 ? kCfg32 : kCfg64;
     const int n = elem == 4 ? (int)(sizeof(kCfg32) / sizeof(ZCfg)) : (int)(sizeof(kCfg64) / sizeof(ZCfg));
-    int first = -1;
     for (int i = 0; i < n; i++)
-        if (zcfg_fits(list[i], K, elem)) {
-            first = i;
-            break;
-        }
-    const char *ov = getenv("SPME_ZFFT_CFG");
-    if (ov && first >= 0) {
-        const int i = atoi(ov);
-        if (i >= 0 && i < n && zcfg_fits(list[i], K, elem)) return i;
-    }
-    return first;
+        if (zcfg_fits(list[i], K, elem)) return i;
+    return -1;
 }
 
 }  // namespace
@@ -560,11 +580,10 @@ bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem) {
     const int W = zfft_width(K, elem);
     if (!fn || W == 0 || ((uintptr_t)G % 16) != 0) return false;
     const int zb = zchunk(K);
-    const int rs = W + (elem == 4 ? 2 : 0);
     const cuuint64_t plane = (cuuint64_t)K * (K / 2 + 1) * 2;  // values per z-plane
     const cuuint64_t dims[3] = {plane, (cuuint64_t)K, (cuuint64_t)C};
     const cuuint64_t strides[2] = {plane * elem, plane * K * elem};
-    const cuuint32_t box[3] = {(cuuint32_t)(2 * rs), (cuuint32_t)zb, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)(2 * W), (cuuint32_t)zb, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
                     3, G, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -573,18 +592,17 @@ bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem) {
     return r == CUDA_SUCCESS;
 }
 
-template <typename T, int W, int MAXP>
-cudaError_t launch_zcfg(const CUtensorMap &map, T *G, const T *tab2, const T *tw, const int *perm,
+template <typename T, int W, int CT, int MINB, int MAXP>
+cudaError_t launch_zcfg(const CUtensorMap &map, const T *tab2, const T *tw, const int *perm,
                         const ZPlan &zp, T twopi_L, int R, int zb, int *err, cudaStream_t s) {
-    auto kern = k_zfft_influence<T, W, MAXP>;
+    auto kern = k_zfft_influence<T, W, CT, MINB, MAXP>;
     const int K = zp.K, Kh = K / 2 + 1;
     const size_t smem = zsmem_bytes<T>(K, W);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid(K, (Kh + W - 1) / W);
-    kern<<<grid, kZThreads, smem, s>>>(map, reinterpret_cast<Cx<T> *>(G), tab2,
-                                       reinterpret_cast<const Cx<T> *>(tw), perm, zp, twopi_L, R,
-                                       zb, err);
+    const int nchunk = (K * Kh + W - 1) / W;
+    kern<<<nchunk, CT + 32, smem, s>>>(map, tab2, reinterpret_cast<const Cx<T> *>(tw), perm, zp,
+                                         twopi_L, R, zb, err);
     return cudaGetLastError();
 }
 
@@ -599,19 +617,21 @@ cudaError_t launch_zfft_influence(const CUtensorMap &map, T *G, const T *tab2, c
     const int zb = zchunk(K);
     cudaError_t e = cudaErrorInvalidValue;
     const ZCfg c = (sizeof(T) == 4 ? kCfg32 : kCfg64)[ci];
-#define SPME_ZCFG(WW, PP)                                                                       \
-    if (c.W == WW && c.maxp == PP)                                                              \
-        e = launch_zcfg<T, WW, PP>(map, G, tab2, tw, perm, zp, twopi_L, R, zb, err, s);
+#define SPME_ZCFG(WW, CC, BB, PP)                                                               \
+    if (c.W == WW && c.ct == CC && c.minb == BB && c.maxp == PP)                                \
+        e = launch_zcfg<T, WW, CC, BB, PP>(map, tab2, tw, perm, zp, twopi_L, R, zb, err, s);
     if constexpr (sizeof(T) == 4) {
-        SPME_ZCFG(16, 12)
-        SPME_ZCFG(8, 12)
-        SPME_ZCFG(4, 12)
-        SPME_ZCFG(2, 12)
+        SPME_ZCFG(16, 384, 1, 12)
+        SPME_ZCFG(8, 192, 2, 12)
+        SPME_ZCFG(16, 192, 1, 24)
+        SPME_ZCFG(4, 192, 1, 24)
+        SPME_ZCFG(2, 192, 1, 24)
     } else {
-        SPME_ZCFG(8, 6)
-        SPME_ZCFG(4, 6)
-        SPME_ZCFG(2, 6)
-        SPME_ZCFG(1, 12)
+        SPME_ZCFG(8, 384, 1, 6)
+        SPME_ZCFG(4, 192, 2, 12)
+        SPME_ZCFG(8, 192, 1, 12)
+        SPME_ZCFG(2, 192, 1, 24)
+        SPME_ZCFG(1, 192, 1, 24)
     }
 #undef SPME_ZCFG
     if (e != cudaSuccess) return e;
