@@ -116,6 +116,14 @@ int spme_stage_times(const spme_t *spme, float *ms, int n);
  * (cuFFT's own kernels are not included). */
 long spme_launch_count(const spme_t *spme);
 
+/* Spread kernel.  1 (default where it applies: K >= 32, at least 12
+ * components, an engine created with max_nrhs >= 4): column gather, each mesh
+ * column visits only the particles whose stencil covers it, force components
+ * across the lanes of a warp.  0: tile kernel, threads own the columns of a
+ * mesh tile and visit every particle staged for the tile.  Mode 1 on an engine
+ * without the column-gather buffers returns SPME_ERR_UNSUPPORTED. */
+int spme_set_spread_mode(spme_t *spme, int mode);
+
 /* Transform strategy of the mesh pass.  1: cuFFT 2D (y, x) transforms of
  * every z-plane, then one fused kernel doing the z transform, the influence
  * and the inverse z transform in shared memory (one pass over the half

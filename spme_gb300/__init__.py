@@ -84,6 +84,7 @@ def load(path: str | None = None):
         "spme_set_tile": (i, [_P, i, i, i]),
         "spme_set_graphs": (i, [_P, i]),
         "spme_set_fft_mode": (i, [_P, i]),
+        "spme_set_spread_mode": (i, [_P, i]),
         "spme_last_error": (i, [_P]),
         "spme_error_string": (ctypes.c_char_p, [i]),
         "cutoff2xi": (None, [d, d, d, ctypes.POINTER(d)]),
@@ -325,6 +326,10 @@ class Engine:
     def set_graphs(self, on: bool = True):
         """Replay captured CUDA graphs for repeated passes (see spme_set_graphs)."""
         _check(load().spme_set_graphs(self.h, 1 if on else 0), "spme_set_graphs")
+
+    def set_spread_mode(self, mode: int):
+        """1: column-gather spread (default where it applies); 0: tile spread."""
+        _check(load().spme_set_spread_mode(self.h, int(mode)), "spme_set_spread_mode")
 
     def set_fft_mode(self, mode: int):
         """1: 2D cuFFT + fused z-FFT/influence kernel (default); 0: 3D cuFFT + influence."""

@@ -79,6 +79,12 @@ struct _spme_t {
     int *d_rec_idx = nullptr;
     uint32_t *d_rec_start = nullptr;
     void *d_rec_w = nullptr;
+    // column-gather spread: records sorted by stencil-start cell (K^3 keys)
+    bool cols = false;
+    int spread_mode = 1;  // 1: column-gather kernel where it applies, 0: tile kernel
+    int *d_scount = nullptr, *d_soff = nullptr, *d_sperm = nullptr, *d_srec_idx = nullptr;
+    uint32_t *d_srec_start = nullptr;
+    void *d_srec_w = nullptr;
     int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
     void *d_cpos = nullptr;  // float4 (FP32 engine) or double4 (FP64 engine)
     void *d_mesh = nullptr, *d_cmesh = nullptr, *d_tab = nullptr;
@@ -243,6 +249,7 @@ int alloc_tiles(spme_t *e) {
     e->d_tcount = e->d_toff = e->d_scan_tmp = nullptr;
     size_t ncell = (size_t)e->nc * e->nc * e->nc;
     size_t nkeys = std::max(need, ncell);
+    if (e->cols) nkeys = std::max(nkeys, (size_t)e->prm.dim * e->prm.dim * e->prm.dim);
     TRY(dalloc(&e->d_tcount, sizeof(int) * need));
     TRY(dalloc(&e->d_toff, sizeof(int) * (need + 1)));
     TRY(dalloc(&e->d_scan_tmp, sizeof(int) * spme::scan_tmp_elems((int)nkeys)));
@@ -362,6 +369,16 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY(dalloc(&e->d_key, sizeof(int) * n));
     TRY(dalloc(&e->d_slot, sizeof(int) * n));
     TRY(dalloc(&e->d_tperm, sizeof(int) * n));
+    e->cols = (prm.terms & SPME_TERM_RECIP) && C >= 12 && spme::spread_cols_ok((int)K, 12, e->elem);
+    if (e->cols) {
+        const size_t K3 = K * K * K;
+        TRY(dalloc(&e->d_scount, sizeof(int) * K3));
+        TRY(dalloc(&e->d_soff, sizeof(int) * (K3 + 1)));
+        TRY(dalloc(&e->d_sperm, sizeof(int) * n));
+        TRY(dalloc(&e->d_srec_idx, sizeof(int) * n));
+        TRY(dalloc(&e->d_srec_start, sizeof(uint32_t) * n));
+        TRY(dalloc(&e->d_srec_w, e->elem * record_width(e) * n));
+    }
     TRY(alloc_tiles(e));
     TRY(dalloc(&e->d_rec_idx, sizeof(int) * n));
     TRY(dalloc(&e->d_rec_start, sizeof(uint32_t) * n));
@@ -500,7 +517,8 @@ void destroy_impl(spme_t *e) {
                     e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_mesh,
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
-                    e->d_zip};
+                    e->d_zip,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
+                    e->d_srec_start, e->d_srec_w};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -536,6 +554,20 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
             spme::launch_records<double>(e->d_pos, e->d_tperm, n, e->g, e->d_rec_idx,
                                          e->d_rec_start, (double *)e->d_rec_w, s);
         e->launches += 6;
+        if (e->cols) {
+            const int K3 = e->g.K * e->g.K * e->g.K;
+            TRY_CUDA(cudaMemsetAsync(e->d_scount, 0, sizeof(int) * K3, s));
+            spme::launch_start_keys(e->d_pos, n, e->g, e->d_key, e->d_scount, e->d_slot, s);
+            spme::launch_scan(e->d_scount, K3, e->d_soff, e->d_scan_tmp, s);
+            spme::launch_scatter(e->d_key, e->d_slot, e->d_soff, n, e->d_sperm, s);
+            if (is_fp32(e))
+                spme::launch_records<float>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
+                                            e->d_srec_start, (float *)e->d_srec_w, s);
+            else
+                spme::launch_records<double>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
+                                             e->d_srec_start, (double *)e->d_srec_w, s);
+            e->launches += 6;
+        }
     }
     if (e->prm.terms & SPME_TERM_REAL) {
         int ncell = e->nc * e->nc * e->nc;
@@ -613,8 +645,13 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         if (!e->d_mesh || !e->d_cmesh || !e->d_tab) return SPME_ERR_STATE;
         PlanPair *pp;
         TRY(get_plans(e, C, &pp));
-        TRY_CUDA(spme::launch_spread<T>(e->d_toff, e->d_rec_idx, e->d_rec_start,
-                                        (const T *)e->d_rec_w, F, C, e->g, (T *)e->d_mesh, s));
+        if (e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem))
+            TRY_CUDA(spme::launch_spread_cols<T>(e->d_soff, e->d_srec_idx, e->d_srec_start,
+                                                 (const T *)e->d_srec_w, F, C, e->g,
+                                                 (T *)e->d_mesh, s));
+        else
+            TRY_CUDA(spme::launch_spread<T>(e->d_toff, e->d_rec_idx, e->d_rec_start,
+                                            (const T *)e->d_rec_w, F, C, e->g, (T *)e->d_mesh, s));
         e->launches++;
         if (prof) cudaEventRecord(e->ev[2], s);
         const bool fused = e->fft_mode == 1 && pp->has2d;
@@ -861,6 +898,16 @@ int spme_set_tile(spme_t *e, int tx, int ty, int tz) {
     e->tile[2] = tz;
     e->have_pos = false;
     drop_graphs(e);
+    return e->last_error = SPME_OK;
+}
+
+int spme_set_spread_mode(spme_t *e, int mode) {
+    if (!e || (mode != 0 && mode != 1)) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    if (mode == 1 && !e->cols) return e->last_error = SPME_ERR_UNSUPPORTED;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    drop_graphs(e);
+    e->spread_mode = mode;
     return e->last_error = SPME_OK;
 }
 

@@ -16,6 +16,9 @@ namespace spme {
 // Tile key of each particle's stencil start, and a slot within its tile.
 void launch_tile_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
                       int *slot, cudaStream_t s);
+// Stencil-start cell key ((sy K + sx) K + sz, K^3 keys) and slot within it.
+void launch_start_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
+                       int *slot, cudaStream_t s);
 // Real-space cell key (nc^3 cells of edge L/nc) and slot within its cell.
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
                       int *slot, cudaStream_t s);
@@ -40,6 +43,14 @@ template <typename T>
 cudaError_t launch_spread(const int *tile_off, const int *rec_idx, const uint32_t *rec_start,
                           const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
                           cudaStream_t s);
+// Column-gather spread (spread_cols.cu): records sorted by stencil-start cell,
+// start_off[(sy K + sx) K + sz] the offsets of that order (K^3 + 1 entries).
+// Usable when spread_cols_ok(K, C, elem).
+bool spread_cols_ok(int K, int C, size_t elem);
+template <typename T>
+cudaError_t launch_spread_cols(const int *start_off, const int *rec_idx,
+                               const uint32_t *rec_start, const T *rec_w, const T *F, int C,
+                               const MeshGeom &g, T *mesh, cudaStream_t s);
 // TMA descriptors of the real mesh [C][K][K][K] for the interpolation halo
 // boxes (4- and 8-component chunks).
 struct InterpMaps {

@@ -27,6 +27,24 @@ __global__ void k_tile_keys(const double *__restrict__ pos, int n, MeshGeom g,
     slot[i] = atomicAdd(&count[k], 1);
 }
 
+// Key of the stencil-start cell in (y, x, z) order, z fastest: for a fixed
+// start column (sy, sx) the particles of a z range are contiguous.
+__global__ void k_start_keys(const double *__restrict__ pos, int n, MeshGeom g,
+                             int *__restrict__ key, int *__restrict__ count,
+                             int *__restrict__ slot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double fr;
+        mesh_coord(pos[3 * i + d], g.L, g.K, g.p, s[d], fr);
+    }
+    int k = (s[1] * g.K + s[0]) * g.K + s[2];
+    key[i] = k;
+    slot[i] = atomicAdd(&count[k], 1);
+}
+
 __global__ void k_cell_keys(const double *__restrict__ pos, int n, double L, int nc,
                             int *__restrict__ key, int *__restrict__ count,
                             int *__restrict__ slot) {
@@ -201,6 +219,11 @@ inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 void launch_tile_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
                       int *slot, cudaStream_t s) {
     if (n > 0) k_tile_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, key, count, slot);
+}
+
+void launch_start_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
+                       int *slot, cudaStream_t s) {
+    if (n > 0) k_start_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, key, count, slot);
 }
 
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,

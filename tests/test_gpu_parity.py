@@ -175,3 +175,32 @@ def test_device_pointer_api(gpu_lib):
     eng.synchronize()
     ref = oracle.full(pos, L, xi, rc, K, p, f, nthreads=4)
     assert relerr(ud.cpu().numpy(), ref) < FP32_TOL
+
+
+# (N, L, K, p, R): even / odd K, all orders, one and two component chunks
+SPREAD_CASES = [
+    (900, 40.0, 32, 6, 4),
+    (1200, 50.0, 45, 4, 5),
+    (700, 36.0, 36, 8, 16),
+    (2000, 60.0, 64, 6, 20),
+]
+
+
+@pytest.mark.parametrize("case", SPREAD_CASES)
+def test_column_gather_spread_matches_tile_spread(gpu_lib, case):
+    """The column-gather spread and the tile spread give the same operator
+    (FP64 to round-off), and both match the oracle."""
+    n, L, K, p, R = case
+    xi = 0.35
+    pos, f = uniform_case(n, L, R, seed=K * p + R)
+    out = {}
+    for mode in (0, 1):
+        eng = spme_gb300.Engine(n, L, xi, K, p, precision="fp64", max_nrhs=R,
+                                terms=spme_gb300.TERM_RECIP)
+        eng.set_spread_mode(mode)
+        eng.set_positions(pos)
+        out[mode] = eng.apply(f)
+        eng.close()
+    assert relerr(out[1], out[0]) < 1e-13
+    ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
+    assert relerr(out[1], ref) < FP64_TOL
