@@ -85,6 +85,7 @@ struct _spme_t {
     int *d_scount = nullptr, *d_soff = nullptr, *d_sperm = nullptr, *d_srec_idx = nullptr;
     uint32_t *d_srec_start = nullptr;
     void *d_srec_w = nullptr;
+    void *d_Fs = nullptr;  // force rows in start-cell order
     int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
     void *d_cpos = nullptr;  // float4 (FP32 engine) or double4 (FP64 engine)
     void *d_mesh = nullptr, *d_cmesh = nullptr, *d_tab = nullptr;
@@ -378,6 +379,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_srec_idx, sizeof(int) * n));
         TRY(dalloc(&e->d_srec_start, sizeof(uint32_t) * n));
         TRY(dalloc(&e->d_srec_w, e->elem * record_width(e) * n));
+        TRY(dalloc(&e->d_Fs, e->elem * C * n));
     }
     TRY(alloc_tiles(e));
     TRY(dalloc(&e->d_rec_idx, sizeof(int) * n));
@@ -518,7 +520,7 @@ void destroy_impl(spme_t *e) {
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
-                    e->d_srec_start, e->d_srec_w};
+                    e->d_srec_start, e->d_srec_w, e->d_Fs};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -645,11 +647,13 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         if (!e->d_mesh || !e->d_cmesh || !e->d_tab) return SPME_ERR_STATE;
         PlanPair *pp;
         TRY(get_plans(e, C, &pp));
-        if (e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem))
-            TRY_CUDA(spme::launch_spread_cols<T>(e->d_soff, e->d_srec_idx, e->d_srec_start,
-                                                 (const T *)e->d_srec_w, F, C, e->g,
-                                                 (T *)e->d_mesh, s));
-        else
+        if (e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem)) {
+            spme::launch_gather_rows<T>(F, e->d_srec_idx, n, C, (T *)e->d_Fs, s);
+            TRY_CUDA(spme::launch_spread_cols<T>(e->d_soff, e->d_srec_start,
+                                                 (const T *)e->d_srec_w, (const T *)e->d_Fs, C,
+                                                 e->g, (T *)e->d_mesh, s));
+            e->launches++;
+        } else
             TRY_CUDA(spme::launch_spread<T>(e->d_toff, e->d_rec_idx, e->d_rec_start,
                                             (const T *)e->d_rec_w, F, C, e->g, (T *)e->d_mesh, s));
         e->launches++;

@@ -44,13 +44,12 @@ cudaError_t launch_spread(const int *tile_off, const int *rec_idx, const uint32_
                           const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
                           cudaStream_t s);
 // Column-gather spread (spread_cols.cu): records sorted by stencil-start cell,
-// start_off[(sy K + sx) K + sz] the offsets of that order (K^3 + 1 entries).
-// Usable when spread_cols_ok(K, C, elem).
+// start_off[(sy K + sx) K + sz] the offsets of that order (K^3 + 1 entries),
+// Fs the force rows in the same order.  Usable when spread_cols_ok(K, C, elem).
 bool spread_cols_ok(int K, int C, size_t elem);
 template <typename T>
-cudaError_t launch_spread_cols(const int *start_off, const int *rec_idx,
-                               const uint32_t *rec_start, const T *rec_w, const T *F, int C,
-                               const MeshGeom &g, T *mesh, cudaStream_t s);
+cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, const T *rec_w,
+                               const T *Fs, int C, const MeshGeom &g, T *mesh, cudaStream_t s);
 // TMA descriptors of the real mesh [C][K][K][K] for the interpolation halo
 // boxes (4- and 8-component chunks).
 struct InterpMaps {
@@ -115,6 +114,9 @@ cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, 
 template <typename T>
 void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s);
 // F[i][3R] = f[r*ld + 3i + d]
+// Fs[s][c] = F[idx[s]][c] for s < n (C components per row).
+template <typename T>
+void launch_gather_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStream_t s);
 template <typename T>
 void launch_pack(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
 // u[r*ld + 3i + d] = beta*u + alpha*W[i][3r+d]   (u not read when beta == 0)

@@ -24,6 +24,19 @@ __global__ void k_pack(const T *__restrict__ f, long ld, int n, int R, T *__rest
     }
 }
 
+// Fs[s][c] = F[idx[s]][c]: force rows in another particle order.
+template <typename T>
+__global__ void k_gather_rows(const T *__restrict__ F, const int *__restrict__ idx, int n, int C,
+                              T *__restrict__ Fs) {
+    const size_t total = (size_t)n * C;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = t / C;
+        const int c = (int)(t - s * C);
+        Fs[t] = F[(size_t)idx[s] * C + c];
+    }
+}
+
 template <typename T>
 __global__ void k_unpack(const T *__restrict__ W, int n, int R, T alpha, T beta,
                          T *__restrict__ u, long ld) {
@@ -66,6 +79,12 @@ void launch_pack(const T *f, long ld, int n, int R, T *F, cudaStream_t s) {
 }
 
 template <typename T>
+void launch_gather_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStream_t s) {
+    size_t total = (size_t)n * C;
+    if (total) k_gather_rows<T><<<blocks_for(total), 256, 0, s>>>(F, idx, n, C, Fs);
+}
+
+template <typename T>
 void launch_unpack(const T *W, int n, int R, double alpha, double beta, T *u, long ld,
                    cudaStream_t s) {
     size_t total = (size_t)n * 3 * R;
@@ -80,6 +99,10 @@ void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s) 
 
 template void launch_self<float>(const float *, int, int, double, float *, cudaStream_t);
 template void launch_self<double>(const double *, int, int, double, double *, cudaStream_t);
+template void launch_gather_rows<float>(const float *, const int *, int, int, float *,
+                                        cudaStream_t);
+template void launch_gather_rows<double>(const double *, const int *, int, int, double *,
+                                         cudaStream_t);
 template void launch_pack<float>(const float *, long, int, int, float *, cudaStream_t);
 template void launch_pack<double>(const double *, long, int, int, double *, cudaStream_t);
 template void launch_unpack<float>(const float *, int, int, double, double, float *, long,

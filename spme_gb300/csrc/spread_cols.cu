@@ -76,16 +76,16 @@ struct WarpScratch {
     static constexpr int NQ = P * (P + 1);
     int begA[NQ], nA[NQ], begB[NQ];
     int pre[NQ + 1];
-    int d[32], idx[32];
+    int d[32], idx[32];  // idx: position in the start-cell order (row of Fs)
     T w0[32], w1[32];  // w_x w_y of the pair's two columns
     T wz[32][P];
 };
 
 template <typename T, int P, int CPL, int TZ, int NW>
-__global__ void __launch_bounds__(NW * 32, (sizeof(T) == 4 ? 2 : 1))
-k_spread_cols(const int *__restrict__ soff, const int *__restrict__ rec_idx,
-              const uint32_t *__restrict__ rec_start, const T *__restrict__ rec_w,
-              const T *__restrict__ F, int C, int K, int nzt, T *__restrict__ mesh) {
+__global__ void __launch_bounds__(NW * 32, (sizeof(T) == 4 ? 3 : 1))
+k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_start,
+              const T *__restrict__ rec_w, const T *__restrict__ Fs, int C, int K, int nzt,
+              T *__restrict__ mesh) {
     constexpr int WS = RecordWidth<T, P>::value;
     constexpr int XT = 2 * NW;          // columns per block
     constexpr int CC = 16 * CPL;        // components per block
@@ -178,7 +178,7 @@ k_spread_cols(const int *__restrict__ soff, const int *__restrict__ rec_idx,
                 ws.w0[lane] = ox < P ? wy * __ldg(rw + ox) : T(0);
                 ws.w1[lane] = (ox1 < P && xa + 1 < K) ? wy * __ldg(rw + ox1) : T(0);
                 ws.d[lane] = sz - (partB ? z0 + K : z0);  // in [-(P-1), ext)
-                ws.idx[lane] = __ldg(rec_idx + s);
+                ws.idx[lane] = s;
                 T wz[P];
                 load_weights<T, P>(rw + 2 * P, wz);
 #pragma unroll
@@ -192,7 +192,7 @@ k_spread_cols(const int *__restrict__ soff, const int *__restrict__ rec_idx,
 #pragma unroll
                 for (int k = 0; k < CPL; k++) {
                     const int c = cb + l16 + 16 * k;
-                    fn[k] = c < C ? __ldg(F + frow + c) : T(0);
+                    fn[k] = c < C ? __ldg(Fs + frow + c) : T(0);
                 }
             }
             for (int j = 0; j < nb; j++) {
@@ -204,7 +204,7 @@ k_spread_cols(const int *__restrict__ soff, const int *__restrict__ rec_idx,
 #pragma unroll
                     for (int k = 0; k < CPL; k++) {
                         const int c = cb + l16 + 16 * k;
-                        fn[k] = c < C ? __ldg(F + frow + c) : T(0);
+                        fn[k] = c < C ? __ldg(Fs + frow + c) : T(0);
                     }
                 }
                 const T wxy = half ? ws.w1[j] : ws.w0[j];
@@ -248,9 +248,8 @@ k_spread_cols(const int *__restrict__ soff, const int *__restrict__ rec_idx,
 }
 
 template <typename T, int P, int CPL>
-cudaError_t launch_cols(const int *soff, const int *rec_idx, const uint32_t *rec_start,
-                        const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
-                        cudaStream_t s) {
+cudaError_t launch_cols(const int *soff, const uint32_t *rec_start, const T *rec_w, const T *Fs,
+                        int C, const MeshGeom &g, T *mesh, cudaStream_t s) {
     constexpr int NW = 8;
     constexpr int TZ = sizeof(T) == 4 ? 16 : 8;
     constexpr int XT = 2 * NW, CC = 16 * CPL;
@@ -262,18 +261,17 @@ cudaError_t launch_cols(const int *soff, const int *rec_idx, const uint32_t *rec
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((K + XT - 1) / XT, K, nzt * nchunk);
-    kern<<<grid, NW * 32, smem, s>>>(soff, rec_idx, rec_start, rec_w, F, C, K, nzt, mesh);
+    kern<<<grid, NW * 32, smem, s>>>(soff, rec_start, rec_w, Fs, C, K, nzt, mesh);
     return cudaGetLastError();
 }
 
 template <typename T, int P>
-cudaError_t dispatch_cpl(const int *soff, const int *rec_idx, const uint32_t *rec_start,
-                         const T *rec_w, const T *F, int C, const MeshGeom &g, T *mesh,
-                         cudaStream_t s) {
+cudaError_t dispatch_cpl(const int *soff, const uint32_t *rec_start, const T *rec_w, const T *Fs,
+                         int C, const MeshGeom &g, T *mesh, cudaStream_t s) {
     // components per lane: the smallest CPL with 16 CPL >= C, at most 3
-    if (C <= 16) return launch_cols<T, P, 1>(soff, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
-    if (C <= 32) return launch_cols<T, P, 2>(soff, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
-    return launch_cols<T, P, 3>(soff, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
+    if (C <= 16) return launch_cols<T, P, 1>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
+    if (C <= 32) return launch_cols<T, P, 2>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
+    return launch_cols<T, P, 3>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
 }
 
 }  // namespace
@@ -287,23 +285,22 @@ bool spread_cols_ok(int K, int C, size_t elem) {
 }
 
 template <typename T>
-cudaError_t launch_spread_cols(const int *start_off, const int *rec_idx,
-                               const uint32_t *rec_start, const T *rec_w, const T *F, int C,
-                               const MeshGeom &g, T *mesh, cudaStream_t s) {
+cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, const T *rec_w,
+                               const T *Fs, int C, const MeshGeom &g, T *mesh, cudaStream_t s) {
     if (!spread_cols_ok(g.K, C, sizeof(T))) return cudaErrorInvalidValue;
     switch (g.p) {
-        case 4: return dispatch_cpl<T, 4>(start_off, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
-        case 6: return dispatch_cpl<T, 6>(start_off, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
-        case 8: return dispatch_cpl<T, 8>(start_off, rec_idx, rec_start, rec_w, F, C, g, mesh, s);
+        case 4: return dispatch_cpl<T, 4>(start_off, rec_start, rec_w, Fs, C, g, mesh, s);
+        case 6: return dispatch_cpl<T, 6>(start_off, rec_start, rec_w, Fs, C, g, mesh, s);
+        case 8: return dispatch_cpl<T, 8>(start_off, rec_start, rec_w, Fs, C, g, mesh, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-template cudaError_t launch_spread_cols<float>(const int *, const int *, const uint32_t *,
-                                               const float *, const float *, int,
-                                               const MeshGeom &, float *, cudaStream_t);
-template cudaError_t launch_spread_cols<double>(const int *, const int *, const uint32_t *,
-                                                const double *, const double *, int,
-                                                const MeshGeom &, double *, cudaStream_t);
+template cudaError_t launch_spread_cols<float>(const int *, const uint32_t *, const float *,
+                                               const float *, int, const MeshGeom &, float *,
+                                               cudaStream_t);
+template cudaError_t launch_spread_cols<double>(const int *, const uint32_t *, const double *,
+                                                const double *, int, const MeshGeom &, double *,
+                                                cudaStream_t);
 
 }  // namespace spme
