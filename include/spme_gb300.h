@@ -103,9 +103,10 @@ int spme_apply(spme_t *spme, int nrhs, double alpha, const void *f, long ldf, do
 int spme_synchronize(spme_t *spme);
 
 /* Per-stage device times (ms) of the last apply when profiling is on.
- * spme_set_profiling(spme, 1): CUDA events around each stage, the real-space
- * sum still overlapping the mesh stages on its own stream; level 2 also runs
- * the real-space sum on the main stream so each stage is timed alone; 0 off.
+ * spme_set_profiling(spme, 1): CUDA events around each stage (with
+ * spme_set_overlap on, the real-space sum still overlaps the mesh stages on its
+ * own stream); level 2 always runs the real-space sum on the main stream so
+ * each stage is timed alone; 0 off.
  * Stages, in order: pack, real-space, spread, forward FFT, influence,
  * backward FFT, interpolate, unpack.  Returns the number of stages written
  * (<= n). */
@@ -115,6 +116,12 @@ int spme_stage_times(const spme_t *spme, float *ms, int n);
 /* Number of this library's kernels the engine has launched since creation
  * (cuFFT's own kernels are not included). */
 long spme_launch_count(const spme_t *spme);
+
+/* Real-space sum concurrent with the mesh pipeline (on = 1: on a second
+ * stream, joined before the interpolation adds onto it) or before it on the
+ * same stream (0, the default: on a full GPU the mesh kernels occupy every SM
+ * and the concurrent sum only slows them down). */
+int spme_set_overlap(spme_t *spme, int on);
 
 /* Spread kernel.  1 (default where it applies: K >= 32, at least 12
  * components, an engine created with max_nrhs >= 4): column gather, each mesh

@@ -85,6 +85,7 @@ def load(path: str | None = None):
         "spme_set_graphs": (i, [_P, i]),
         "spme_set_fft_mode": (i, [_P, i]),
         "spme_set_spread_mode": (i, [_P, i]),
+        "spme_set_overlap": (i, [_P, i]),
         "spme_last_error": (i, [_P]),
         "spme_error_string": (ctypes.c_char_p, [i]),
         "cutoff2xi": (None, [d, d, d, ctypes.POINTER(d)]),
@@ -326,6 +327,10 @@ class Engine:
     def set_graphs(self, on: bool = True):
         """Replay captured CUDA graphs for repeated passes (see spme_set_graphs)."""
         _check(load().spme_set_graphs(self.h, 1 if on else 0), "spme_set_graphs")
+
+    def set_overlap(self, on: bool):
+        """Real-space sum concurrent with the mesh pipeline (True) or before it."""
+        _check(load().spme_set_overlap(self.h, 1 if on else 0), "spme_set_overlap")
 
     def set_spread_mode(self, mode: int):
         """1: column-gather spread (default where it applies); 0: tile spread."""

@@ -62,6 +62,9 @@ struct _spme_t {
     cudaEvent_t ev[kStages + 1] = {};
     cudaEvent_t ev_rs[2] = {};
     float stage_ms[kStages] = {};
+    bool ran_serial = false;  // last profiled pass ran the real-space sum on the main stream
+    // real-space sum concurrent with the mesh pipeline (aux stream) or before it
+    int overlap = 0;
     bool stages_valid = false;
     bool ran_real = false;
     long launches = 0;
@@ -94,6 +97,7 @@ struct _spme_t {
     size_t work_bytes = 0;
     std::vector<PlanPair> plans;
     void *d_F = nullptr, *d_W = nullptr, *d_fstage = nullptr, *d_ustage = nullptr;
+    void *d_W2 = nullptr;  // mesh part of the result when the real-space part is in d_W
     int *d_err = nullptr;  // device-side error flag (TMA wait timeouts)
     // FFT mode 1: 2D cuFFT + fused z-FFT/influence kernel; 0: 3D cuFFT + influence
     int fft_mode = 1;
@@ -437,6 +441,8 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY_CUDA(cudaMemsetAsync(e->d_err, 0, sizeof(int), e->stream));
     TRY(dalloc(&e->d_F, e->elem * n * C));
     TRY(dalloc(&e->d_W, e->elem * n * C));
+    if ((prm.terms & SPME_TERM_RECIP) && (prm.terms & (SPME_TERM_REAL | SPME_TERM_SELF)))
+        TRY(dalloc(&e->d_W2, e->elem * n * C));
     TRY(dalloc(&e->d_fstage, e->elem * n * C));
     TRY(dalloc(&e->d_ustage, e->elem * n * C));
     TRY_CUDA(cudaStreamSynchronize(e->stream));
@@ -520,7 +526,7 @@ void destroy_impl(spme_t *e) {
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
-                    e->d_srec_start, e->d_srec_w, e->d_Fs};
+                    e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -619,9 +625,10 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
     spme::launch_pack<T>(f, ldf, n, R, F, s);
     e->launches++;
     if (prof) cudaEventRecord(e->ev[1], s);
-    // the real-space sum overlaps the mesh pipeline on the aux stream; at
-    // profiling level 2 it runs on the main stream so every stage is timed alone
-    const bool serial = e->profiling >= 2;
+    // the real-space sum runs before the mesh pipeline on the main stream, or
+    // (overlap on) concurrently on the aux stream; at profiling level 2 always
+    // on the main stream so every stage is timed alone
+    const bool serial = e->profiling >= 2 || !e->overlap;
     cudaStream_t rss = serial ? s : e->aux;
     if (rs) {
         if (!serial) {
@@ -683,7 +690,6 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
             TRY_FFT(cufftExecZ2D(bwd, (cufftDoubleComplex *)e->d_cmesh,
                                  (cufftDoubleReal *)e->d_mesh));
         if (prof) cudaEventRecord(e->ev[5], s);
-        if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
         if (pp->maps_tile[0] != e->g.tx || pp->maps_tile[1] != e->g.ty ||
             pp->maps_tile[2] != e->g.tz) {
             spme::make_interp_maps(&pp->maps, e->d_mesh, C, e->g, e->elem);
@@ -691,20 +697,31 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
             pp->maps_tile[1] = e->g.ty;
             pp->maps_tile[2] = e->g.tz;
         }
+        // the mesh part goes to its own buffer when W holds the real-space part:
+        // no read-modify-write (and no wait for the real-space sum) in the
+        // interpolation; the unpack adds the two
+        T *Wm = rs ? (T *)e->d_W2 : W;
+        if (!Wm) return SPME_ERR_STATE;
         TRY_CUDA(spme::launch_interp<T>(pp->maps, e->d_toff, n, e->d_rec_idx, e->d_rec_start,
-                                        (const T *)e->d_rec_w, (const T *)e->d_mesh, C, e->g, W,
-                                        rs ? 1 : 0, e->d_err, s));
+                                        (const T *)e->d_rec_w, (const T *)e->d_mesh, C, e->g, Wm,
+                                        0, e->d_err, s));
         e->launches++;
         if (prof) cudaEventRecord(e->ev[6], s);
+        if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
+        if (rs)
+            spme::launch_unpack_sum<T>(W, Wm, n, R, alpha, beta, u, ldu, s);
+        else
+            spme::launch_unpack<T>(W, n, R, alpha, beta, u, ldu, s);
     } else {
         TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
         if (prof)
             for (int k = 2; k <= 6; k++) cudaEventRecord(e->ev[k], s);
+        spme::launch_unpack<T>(W, n, R, alpha, beta, u, ldu, s);
     }
-    spme::launch_unpack<T>(W, n, R, alpha, beta, u, ldu, s);
     e->launches++;
     if (prof) cudaEventRecord(e->ev[7], s);
     e->ran_real = rs;
+    e->ran_serial = serial;
     e->stages_valid = prof;
     return from_cuda(cudaGetLastError());
 }
@@ -872,7 +889,8 @@ int spme_stage_times(const spme_t *e, float *ms, int n) {
     DeviceGuard dg(e->device);
     cudaEventSynchronize(e->ev[kStages - 1]);
     float t[kStages] = {};
-    cudaEventElapsedTime(&t[0], e->ev[0], e->ev[1]);
+    // serial: ev[1] was re-recorded after the real-space sum, which starts at ev_rs[0]
+    cudaEventElapsedTime(&t[0], e->ev[0], (e->ran_real && e->ran_serial) ? e->ev_rs[0] : e->ev[1]);
     if (e->ran_real) cudaEventElapsedTime(&t[1], e->ev_rs[0], e->ev_rs[1]);
     for (int k = 2; k < kStages; k++) {
         int from = k == 2 ? 1 : k - 1;
@@ -902,6 +920,15 @@ int spme_set_tile(spme_t *e, int tx, int ty, int tz) {
     e->tile[2] = tz;
     e->have_pos = false;
     drop_graphs(e);
+    return e->last_error = SPME_OK;
+}
+
+int spme_set_overlap(spme_t *e, int on) {
+    if (!e) return SPME_ERR_INVALID;
+    DeviceGuard dg(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    drop_graphs(e);
+    e->overlap = on ? 1 : 0;
     return e->last_error = SPME_OK;
 }
 

@@ -54,6 +54,25 @@ __global__ void k_unpack(const T *__restrict__ W, int n, int R, T alpha, T beta,
     }
 }
 
+// u = alpha (W + W2) + beta u: the real-space and mesh parts of the operator.
+template <typename T>
+__global__ void k_unpack_sum(const T *__restrict__ W, const T *__restrict__ W2, int n, int R,
+                             T alpha, T beta, T *__restrict__ u, long ld) {
+    const size_t total = (size_t)n * 3 * R;
+    const int C = 3 * R;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(t / ((size_t)3 * n));
+        const size_t q = t - (size_t)r * 3 * n;
+        const size_t i = q / 3;
+        const int d = (int)(q - i * 3);
+        const size_t k = i * C + 3 * r + d;
+        const T w = W[k] + W2[k];
+        T *o = u + (size_t)r * ld + q;
+        *o = beta == T(0) ? alpha * w : beta * *o + alpha * w;
+    }
+}
+
 template <typename T>
 __global__ void k_self(const T *__restrict__ F, size_t total, T self_c, T *__restrict__ W) {
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
@@ -92,11 +111,23 @@ void launch_unpack(const T *W, int n, int R, double alpha, double beta, T *u, lo
 }
 
 template <typename T>
+void launch_unpack_sum(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
+                       long ld, cudaStream_t s) {
+    size_t total = (size_t)n * 3 * R;
+    if (total)
+        k_unpack_sum<T><<<blocks_for(total), 256, 0, s>>>(W, W2, n, R, (T)alpha, (T)beta, u, ld);
+}
+
+template <typename T>
 void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s) {
     size_t total = (size_t)n * 3 * R;
     if (total) k_self<T><<<blocks_for(total), 256, 0, s>>>(F, total, (T)self_c, W);
 }
 
+template void launch_unpack_sum<float>(const float *, const float *, int, int, double, double,
+                                       float *, long, cudaStream_t);
+template void launch_unpack_sum<double>(const double *, const double *, int, int, double, double,
+                                        double *, long, cudaStream_t);
 template void launch_self<float>(const float *, int, int, double, float *, cudaStream_t);
 template void launch_self<double>(const double *, int, int, double, double *, cudaStream_t);
 template void launch_gather_rows<float>(const float *, const int *, int, int, float *,
