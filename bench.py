@@ -55,8 +55,8 @@ def algorithmic_bytes(w, s=4):
     K, N, C = w["K"], w["N"], 3 * w["R"]
     Kr, Kc = K ** 3, K * K * (K // 2 + 1)
     return {
-        "spread": C * s * Kr,                      # mesh written once
-        "influence": C * 4 * s * Kc + s * Kc,      # complex mesh read+write, table once
+        "spread": C * s * Kr + s * C * N,          # mesh written once, forces read
+        "influence": C * 4 * s * Kc + 2 * s * Kc,  # complex mesh read+write, table once
         "interp": C * s * Kr + s * C * N,          # mesh read once, result written
     }
 
@@ -240,7 +240,11 @@ def run_gb300(args, w):
     f_d = torch.tensor(f, device="cuda")
     u_d = torch.zeros_like(f_d)
     tune = None
-    if not args.no_autotune:
+    if args.tile:
+        tile = tuple(int(v) for v in args.tile.split(","))
+        eng.set_tile(*tile)
+        tune = {"tile": list(tile), "fixed": True}
+    elif not args.no_autotune:
         # tile shape measured on this device (outside the timed region, not cached)
         from spme_gb300.autotune import autotune
         tile, timings = autotune(eng, pos_d, f_d, reps=2, use_cache=False)
@@ -465,6 +469,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tile", default=None,
+                    help="fixed mesh tile 'tx,ty,tz' instead of autotuning (e.g. for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

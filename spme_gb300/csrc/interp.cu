@@ -112,10 +112,29 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
             }
             __syncthreads();
         }
-        for (int s = pbeg + warp; s < pend; s += kThreads / 32) {
-            const T wreg = lane < 3 * P ? rec_w[(size_t)s * WS + lane] : T(0);
+        // the next particle's record is loaded while this one is interpolated
+        constexpr int kWarps = kThreads / 32;
+        T wreg_n = T(0);
+        uint32_t st_n = 0;
+        int idx_n = 0;
+        if (pbeg + warp < pend) {
+            const int s = pbeg + warp;
+            wreg_n = lane < 3 * P ? __ldg(rec_w + (size_t)s * WS + lane) : T(0);
+            st_n = __ldg(rec_start + s);
+            idx_n = __ldg(rec_idx + s);
+        }
+        for (int s = pbeg + warp; s < pend; s += kWarps) {
+            const T wreg = wreg_n;
+            const uint32_t st = st_n;
+            const int idx = idx_n;
+            if (s + kWarps < pend) {
+                const int sn = s + kWarps;
+                wreg_n = lane < 3 * P ? __ldg(rec_w + (size_t)sn * WS + lane) : T(0);
+                st_n = __ldg(rec_start + sn);
+                idx_n = __ldg(rec_idx + sn);
+            }
             int sx, sy, sz;
-            unpack_start(rec_start[s], sx, sy, sz);
+            unpack_start(st, sx, sy, sz);
             const int lx = sx - ox, ly = sy - oy, lz = sz - oz;  // own tile: no wrap
             const T wxv = __shfl_sync(0xffffffffu, wreg, xs < P ? xs : P - 1);
             const T wx = xs < P ? wxv : T(0);
@@ -143,7 +162,7 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
 #pragma unroll
                 for (int o = 4; o < 32; o <<= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
             if (xs == 0) {
-                T *out = W + (size_t)rec_idx[s] * C + c0;
+                T *out = W + (size_t)idx * C + c0;
 #pragma unroll
                 for (int k = 0; k < NG; k++) {
                     const int c = 4 * k + cl;
