@@ -45,9 +45,16 @@ WORKLOADS = {
     "uneven_batch": dict(count=64, R=4, xi=0.3, rc=10.0, a=1.0),
 }
 
-# DRAM bytes per launch measured with ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) for the large workload; None until captured.
-NCU_TRAFFIC = {}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) measured with
+# ncu at full size on the large workload, FP32, R = 16, tile 16x8x8 (a 1-pass metric
+# set); the command is in profiles/dram_large_fp32_r16.md.
+NCU_TRAFFIC = {
+    "large": {
+        "spread": 816367104 + 3164926464,      # k_spread_cols
+        "influence": 3329840128 + 3266490624,  # k_zfft_influence
+        "interp": 6412758016 + 195079680,      # k_interp
+    },
+}
 
 
 def algorithmic_bytes(w, s=4):
@@ -366,7 +373,7 @@ def run_gb300(args, w):
     dom = max(("spread", "influence", "interp"), key=lambda k: kern.get(k, {}).get("ms", 0.0))
     roof = None
     if dom in kern:
-        tr = NCU_TRAFFIC.get(dom)
+        tr = NCU_TRAFFIC.get(args.workload, {}).get(dom)
         roof = {"kernel": dom, "bound": "hbm", "achieved": kern[dom]["achieved_gbs"],
                 "peak": peak, "unit": "GB/s", "frac": kern[dom]["achieved_gbs"] / peak,
                 "traffic": tr, "peak_kind": peak_kind}

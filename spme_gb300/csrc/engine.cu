@@ -622,7 +622,7 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
     const bool prof = e->profiling;
     T *F = (T *)e->d_F, *W = (T *)e->d_W;
     if (prof) cudaEventRecord(e->ev[0], s);
-    spme::launch_pack<T>(f, ldf, n, R, F, s);
+    spme::launch_pack_tiled<T>(f, ldf, n, R, F, s);
     e->launches++;
     if (prof) cudaEventRecord(e->ev[1], s);
     // the real-space sum runs before the mesh pipeline on the main stream, or
@@ -708,15 +708,12 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         e->launches++;
         if (prof) cudaEventRecord(e->ev[6], s);
         if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
-        if (rs)
-            spme::launch_unpack_sum<T>(W, Wm, n, R, alpha, beta, u, ldu, s);
-        else
-            spme::launch_unpack<T>(W, n, R, alpha, beta, u, ldu, s);
+        spme::launch_unpack_tiled<T>(W, rs ? Wm : nullptr, n, R, alpha, beta, u, ldu, s);
     } else {
         TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
         if (prof)
             for (int k = 2; k <= 6; k++) cudaEventRecord(e->ev[k], s);
-        spme::launch_unpack<T>(W, n, R, alpha, beta, u, ldu, s);
+        spme::launch_unpack_tiled<T>(W, nullptr, n, R, alpha, beta, u, ldu, s);
     }
     e->launches++;
     if (prof) cudaEventRecord(e->ev[7], s);

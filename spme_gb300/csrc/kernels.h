@@ -120,10 +120,13 @@ void launch_gather_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStr
 template <typename T>
 void launch_pack(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
 // u[r*ld + 3i + d] = beta*u + alpha*W[i][3r+d]   (u not read when beta == 0)
-// u = alpha (W + W2) + beta u (same layouts as launch_unpack).
+// Tiled (shared-memory) forms of launch_pack / launch_unpack(_sum): coalesced on
+// both sides; W2 may be null (plain unpack).  Up to 48 KB of shared memory.
 template <typename T>
-void launch_unpack_sum(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
-                       long ld, cudaStream_t s);
+void launch_pack_tiled(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
+template <typename T>
+void launch_unpack_tiled(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
+                         long ld, cudaStream_t s);
 template <typename T>
 void launch_unpack(const T *W, int n, int R, double alpha, double beta, T *u, long ld,
                    cudaStream_t s);

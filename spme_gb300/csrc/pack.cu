@@ -54,22 +54,58 @@ __global__ void k_unpack(const T *__restrict__ W, int n, int R, T alpha, T beta,
     }
 }
 
-// u = alpha (W + W2) + beta u: the real-space and mesh parts of the operator.
+// Tiled forms: a block moves pb particles at a time (at most 32, fewer for very
+// many right-hand sides so the tile stays within 48 KB) through shared memory
+// so both sides are coalesced (rows of 3 pb values per right-hand side on the
+// caller's side, rows of C values per particle on the packed side).
+constexpr int kPB = 32;
+
 template <typename T>
-__global__ void k_unpack_sum(const T *__restrict__ W, const T *__restrict__ W2, int n, int R,
-                             T alpha, T beta, T *__restrict__ u, long ld) {
-    const size_t total = (size_t)n * 3 * R;
-    const int C = 3 * R;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const int r = (int)(t / ((size_t)3 * n));
-        const size_t q = t - (size_t)r * 3 * n;
-        const size_t i = q / 3;
-        const int d = (int)(q - i * 3);
-        const size_t k = i * C + 3 * r + d;
-        const T w = W[k] + W2[k];
-        T *o = u + (size_t)r * ld + q;
-        *o = beta == T(0) ? alpha * w : beta * *o + alpha * w;
+__global__ void __launch_bounds__(256)
+k_pack_tiled(const T *__restrict__ f, long ld, int n, int R, int pb, T *__restrict__ F) {
+    extern __shared__ __align__(16) unsigned char pk_raw[];
+    T *tile = reinterpret_cast<T *>(pk_raw);  // [pb][C + 1]
+    const int C = 3 * R, CS = C + 1;
+    for (int i0 = blockIdx.x * pb; i0 < n; i0 += gridDim.x * pb) {
+        const int np = min(pb, n - i0);
+        for (int t = threadIdx.x; t < R * 3 * np; t += blockDim.x) {
+            const int r = t / (3 * np), q = t - r * 3 * np;
+            const int p = q / 3, d = q - p * 3;
+            tile[p * CS + 3 * r + d] = f[(size_t)r * ld + (size_t)3 * i0 + q];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < np * C; t += blockDim.x) {
+            const int p = t / C, c = t - p * C;
+            F[(size_t)(i0 + p) * C + c] = tile[p * CS + c];
+        }
+        __syncthreads();
+    }
+}
+
+// u = alpha (W [+ W2]) + beta u, tiled as k_pack_tiled.
+template <typename T, bool SUM>
+__global__ void __launch_bounds__(256)
+k_unpack_tiled(const T *__restrict__ W, const T *__restrict__ W2, int n, int R, int pb, T alpha,
+               T beta, T *__restrict__ u, long ld) {
+    extern __shared__ __align__(16) unsigned char pk_raw[];
+    T *tile = reinterpret_cast<T *>(pk_raw);  // [pb][C + 1]
+    const int C = 3 * R, CS = C + 1;
+    for (int i0 = blockIdx.x * pb; i0 < n; i0 += gridDim.x * pb) {
+        const int np = min(pb, n - i0);
+        for (int t = threadIdx.x; t < np * C; t += blockDim.x) {
+            const int p = t / C, c = t - p * C;
+            const size_t k = (size_t)(i0 + p) * C + c;
+            tile[p * CS + c] = SUM ? W[k] + W2[k] : W[k];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < R * 3 * np; t += blockDim.x) {
+            const int r = t / (3 * np), q = t - r * 3 * np;
+            const int p = q / 3, d = q - p * 3;
+            const T w = tile[p * CS + 3 * r + d];
+            T *o = u + (size_t)r * ld + (size_t)3 * i0 + q;
+            *o = beta == T(0) ? alpha * w : beta * *o + alpha * w;
+        }
+        __syncthreads();
     }
 }
 
@@ -110,12 +146,40 @@ void launch_unpack(const T *W, int n, int R, double alpha, double beta, T *u, lo
     if (total) k_unpack<T><<<blocks_for(total), 256, 0, s>>>(W, n, R, (T)alpha, (T)beta, u, ld);
 }
 
+int tiled_blocks(int n, int pb) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int need = (n + pb - 1) / pb;
+    return need < sms * 8 ? (need > 0 ? need : 1) : sms * 8;
+}
+
+int tile_particles(int R, size_t elem) {
+    const size_t row = (size_t)(3 * R + 1) * elem;
+    const size_t pb = (size_t)48 * 1024 / row;
+    return (int)(pb < 1 ? 1 : (pb > (size_t)kPB ? kPB : pb));
+}
+
 template <typename T>
-void launch_unpack_sum(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
-                       long ld, cudaStream_t s) {
-    size_t total = (size_t)n * 3 * R;
-    if (total)
-        k_unpack_sum<T><<<blocks_for(total), 256, 0, s>>>(W, W2, n, R, (T)alpha, (T)beta, u, ld);
+void launch_pack_tiled(const T *f, long ld, int n, int R, T *F, cudaStream_t s) {
+    if (n <= 0 || R <= 0) return;
+    const int pb = tile_particles(R, sizeof(T));
+    const size_t smem = (size_t)pb * (3 * R + 1) * sizeof(T);
+    k_pack_tiled<T><<<tiled_blocks(n, pb), 256, smem, s>>>(f, ld, n, R, pb, F);
+}
+
+template <typename T>
+void launch_unpack_tiled(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
+                         long ld, cudaStream_t s) {
+    if (n <= 0 || R <= 0) return;
+    const int pb = tile_particles(R, sizeof(T));
+    const size_t smem = (size_t)pb * (3 * R + 1) * sizeof(T);
+    if (W2)
+        k_unpack_tiled<T, true><<<tiled_blocks(n, pb), 256, smem, s>>>(W, W2, n, R, pb, (T)alpha,
+                                                                        (T)beta, u, ld);
+    else
+        k_unpack_tiled<T, false><<<tiled_blocks(n, pb), 256, smem, s>>>(W, W, n, R, pb, (T)alpha,
+                                                                         (T)beta, u, ld);
 }
 
 template <typename T>
@@ -124,10 +188,12 @@ void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s) 
     if (total) k_self<T><<<blocks_for(total), 256, 0, s>>>(F, total, (T)self_c, W);
 }
 
-template void launch_unpack_sum<float>(const float *, const float *, int, int, double, double,
-                                       float *, long, cudaStream_t);
-template void launch_unpack_sum<double>(const double *, const double *, int, int, double, double,
-                                        double *, long, cudaStream_t);
+template void launch_pack_tiled<float>(const float *, long, int, int, float *, cudaStream_t);
+template void launch_pack_tiled<double>(const double *, long, int, int, double *, cudaStream_t);
+template void launch_unpack_tiled<float>(const float *, const float *, int, int, double, double,
+                                         float *, long, cudaStream_t);
+template void launch_unpack_tiled<double>(const double *, const double *, int, int, double,
+                                          double, double *, long, cudaStream_t);
 template void launch_self<float>(const float *, int, int, double, float *, cudaStream_t);
 template void launch_self<double>(const double *, int, int, double, double *, cudaStream_t);
 template void launch_gather_rows<float>(const float *, const int *, int, int, float *,

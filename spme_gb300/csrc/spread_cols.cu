@@ -31,7 +31,8 @@ template <typename T> struct V16;
 template <> struct V16<float> { using type = float4; };
 template <> struct V16<double> { using type = double2; };
 
-// p weights from a 16-byte aligned address (vector loads where they fit).
+// p weights from a 16-byte aligned address, global or shared (vector loads
+// where they fit).
 template <typename T, int P>
 __device__ __forceinline__ void load_weights(const T *__restrict__ src, T (&w)[P]) {
     constexpr int VW = 16 / (int)sizeof(T);
@@ -39,7 +40,7 @@ __device__ __forceinline__ void load_weights(const T *__restrict__ src, T (&w)[P
     using V = typename V16<T>::type;
 #pragma unroll
     for (int v = 0; v < NV; v++) {
-        const V q = __ldg(reinterpret_cast<const V *>(src) + v);
+        const V q = reinterpret_cast<const V *>(src)[v];
         if constexpr (VW == 4) {
             w[4 * v] = q.x;
             w[4 * v + 1] = q.y;
@@ -51,20 +52,19 @@ __device__ __forceinline__ void load_weights(const T *__restrict__ src, T (&w)[P
         }
     }
 #pragma unroll
-    for (int j = NV * VW; j < P; j++) w[j] = __ldg(src + j);
+    for (int j = NV * VW; j < P; j++) w[j] = src[j];
 }
 
-// acc[D + j] += (wxy wz[j]) f for the planes D + j inside [0, TZ).
+// acc[D + j] += wt[j] f for the planes D + j inside [0, TZ) (wt[j] = w_x w_y w_z[j]).
 template <typename T, int P, int CPL, int TZ, int D>
-__device__ __forceinline__ void add_planes(T (&acc)[TZ][CPL], T wxy, const T (&wz)[P],
+__device__ __forceinline__ void add_planes(T (&acc)[TZ][CPL], const T (&wt)[P],
                                            const T (&f)[CPL]) {
 #pragma unroll
     for (int j = 0; j < P; j++) {
         constexpr int lo = D < 0 ? -D : 0;
         if (j >= lo && D + j < TZ) {
-            const T wv = wxy * wz[j];
 #pragma unroll
-            for (int k = 0; k < CPL; k++) acc[D + j][k] += wv * f[k];
+            for (int k = 0; k < CPL; k++) acc[D + j][k] += wt[j] * f[k];
         }
     }
 }
@@ -74,11 +74,13 @@ __device__ __forceinline__ void add_planes(T (&acc)[TZ][CPL], T wxy, const T (&w
 template <typename T, int P>
 struct WarpScratch {
     static constexpr int NQ = P * (P + 1);
+    static constexpr int PW = (P * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T);  // padded P
+    // staged visit: w_x w_y w_z[j] for the pair's two columns (16-byte rows), then
+    // (z offset, row of Fs)
+    __align__(16) T wt[32][2][PW];
+    int2 dz_row[32];
     int begA[NQ], nA[NQ], begB[NQ];
     int pre[NQ + 1];
-    int d[32], idx[32];  // idx: position in the start-cell order (row of Fs)
-    T w0[32], w1[32];  // w_x w_y of the pair's two columns
-    T wz[32][P];
 };
 
 template <typename T, int P, int CPL, int TZ, int NW>
@@ -91,7 +93,9 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
     constexpr int CC = 16 * CPL;        // components per block
     constexpr int NX = P + 1;           // start columns per column pair (x)
     constexpr int NQ = P * NX;          // start columns per column pair (x and y)
-    constexpr int ROW = TZ * XT + 1;    // shared stride per component (padded)
+    // shared stride per component, padded so the two half-warps' column stores fall
+    // on different banks (even / odd words in FP32)
+    constexpr int ROW = TZ * XT + (sizeof(T) == 4 ? 2 : 1);
     static_assert(-(P - 1) >= -7 && TZ <= 16, "jump table covers offsets -7 .. 15");
     extern __shared__ __align__(16) unsigned char sp_raw[];
     T *tsm = reinterpret_cast<T *>(sp_raw);  // [CC][ROW] transpose buffer
@@ -175,20 +179,22 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 // column xa covered when ox < P, column xa + 1 when ox + 1 < P
                 // (or ox = K - 1: the stencil starts at xa + 1)
                 const int ox1 = ox + 1 == K ? 0 : ox + 1;
-                ws.w0[lane] = ox < P ? wy * __ldg(rw + ox) : T(0);
-                ws.w1[lane] = (ox1 < P && xa + 1 < K) ? wy * __ldg(rw + ox1) : T(0);
-                ws.d[lane] = sz - (partB ? z0 + K : z0);  // in [-(P-1), ext)
-                ws.idx[lane] = s;
+                const T w0 = ox < P ? wy * __ldg(rw + ox) : T(0);
+                const T w1 = (ox1 < P && xa + 1 < K) ? wy * __ldg(rw + ox1) : T(0);
+                ws.dz_row[lane] = make_int2(sz - (partB ? z0 + K : z0), s);  // dz in [-(P-1), ext)
                 T wz[P];
                 load_weights<T, P>(rw + 2 * P, wz);
 #pragma unroll
-                for (int j = 0; j < P; j++) ws.wz[lane][j] = wz[j];
+                for (int j = 0; j < WarpScratch<T, P>::PW; j++) {
+                    ws.wt[lane][0][j] = j < P ? w0 * wz[j] : T(0);
+                    ws.wt[lane][1][j] = j < P ? w1 * wz[j] : T(0);
+                }
             }
             __syncwarp();
             // accumulate the batch (force row of the next visit prefetched)
             T fn[CPL];
             {
-                const size_t frow = (size_t)ws.idx[0] * C;
+                const size_t frow = (size_t)ws.dz_row[0].y * C;
 #pragma unroll
                 for (int k = 0; k < CPL; k++) {
                     const int c = cb + l16 + 16 * k;
@@ -199,22 +205,21 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 T f[CPL];
 #pragma unroll
                 for (int k = 0; k < CPL; k++) f[k] = fn[k];
+                const int2 dr = ws.dz_row[j];
                 if (j + 1 < nb) {
-                    const size_t frow = (size_t)ws.idx[j + 1] * C;
+                    const size_t frow = (size_t)ws.dz_row[j + 1].y * C;
 #pragma unroll
                     for (int k = 0; k < CPL; k++) {
                         const int c = cb + l16 + 16 * k;
                         fn[k] = c < C ? __ldg(Fs + frow + c) : T(0);
                     }
                 }
-                const T wxy = half ? ws.w1[j] : ws.w0[j];
-                T wz[P];
-#pragma unroll
-                for (int q = 0; q < P; q++) wz[q] = ws.wz[j][q];
-                switch (ws.d[j]) {
+                T wt[P];
+                load_weights<T, P>(&ws.wt[j][half][0], wt);
+                switch (dr.x) {
 #define SPME_SPC(DD)                                                                      \
     case DD:                                                                              \
-        if constexpr (DD >= -(P - 1) && DD < TZ) add_planes<T, P, CPL, TZ, DD>(acc, wxy, wz, f); \
+        if constexpr (DD >= -(P - 1) && DD < TZ) add_planes<T, P, CPL, TZ, DD>(acc, wt, f); \
         break;
                     SPME_SPC(-7) SPME_SPC(-6) SPME_SPC(-5) SPME_SPC(-4) SPME_SPC(-3)
                     SPME_SPC(-2) SPME_SPC(-1) SPME_SPC(0) SPME_SPC(1) SPME_SPC(2)
@@ -255,7 +260,8 @@ cudaError_t launch_cols(const int *soff, const uint32_t *rec_start, const T *rec
     constexpr int XT = 2 * NW, CC = 16 * CPL;
     const int K = g.K;
     const int nzt = (K + TZ - 1) / TZ, nchunk = (C + CC - 1) / CC;
-    const size_t smem = (((size_t)CC * (TZ * XT + 1) * sizeof(T) + 15) & ~(size_t)15) +
+    const size_t smem = (((size_t)CC * (TZ * XT + (sizeof(T) == 4 ? 2 : 1)) * sizeof(T) + 15) &
+                         ~(size_t)15) +
                         NW * sizeof(WarpScratch<T, P>);
     auto kern = k_spread_cols<T, P, CPL, TZ, NW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
