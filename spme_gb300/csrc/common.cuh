@@ -16,6 +16,7 @@ struct MeshGeom {
     int tx, ty, tz;        // tile edge per axis
     int ntx, nty, ntz;     // tiles per axis (last one may be short)
     double L;              // box edge
+    double invL;           // 1 / L
 };
 
 // Record width (elements of T) for p weights per axis, padded so each
@@ -57,14 +58,25 @@ __device__ __forceinline__ void bspline_weights(T w, T (&out)[P]) {
 
 // Fractional mesh coordinate of position x (wrapped into [0, L)), following
 // old-version/spme.c:235-256: c = x/L*K, start = floor(c) - p/2 + 1 (mod K).
-__device__ __forceinline__ void mesh_coord(double x, double L, int K, int p, int &start,
-                                           double &frac) {
-    double xw = x - L * floor(x / L);
-    double c = xw / L * (double)K;
+// Multiplies by 1/L (FP64 division is slow); every kernel that needs a
+// particle's stencil start calls this same function, so sort keys and records
+// agree.
+__device__ __forceinline__ void mesh_coord(double x, double L, double invL, int K, int p,
+                                           int &start, double &frac) {
+    double xw = x - L * floor(x * invL);
+    double c = xw * invL * (double)K;
     double fl = floor(c);
     frac = c - fl;
     int s = (int)fl - p / 2 + 1;
     start = pmod(s, K);
+}
+
+// Real-space cell (nc cells of edge L/nc per axis) of coordinate x, and x
+// wrapped into [0, L); shared by the cell keys and the cell-relative positions.
+__device__ __forceinline__ int cell_coord(double x, double L, double invL, int nc, double &xw) {
+    xw = x - L * floor(x * invL);
+    const int v = (int)(xw * invL * (double)nc);
+    return v >= nc ? nc - 1 : (v < 0 ? 0 : v);
 }
 
 __device__ __forceinline__ uint32_t pack_start(int sx, int sy, int sz) {

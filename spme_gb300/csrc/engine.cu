@@ -77,6 +77,7 @@ struct _spme_t {
     bool have_pos = false;
     // device buffers
     double *d_pos = nullptr;
+    int *d_key2 = nullptr, *d_slot2 = nullptr, *d_key3 = nullptr, *d_slot3 = nullptr;
     int *d_key = nullptr, *d_slot = nullptr, *d_tcount = nullptr, *d_toff = nullptr,
         *d_tperm = nullptr, *d_scan_tmp = nullptr;
     int *d_rec_idx = nullptr;
@@ -231,6 +232,7 @@ void set_geometry(spme_t *e) {
     g.K = e->prm.dim;
     g.p = e->prm.porder;
     g.L = e->prm.box_size;
+    g.invL = 1.0 / e->prm.box_size;
     g.tx = std::min(e->tile[0], g.K);
     g.ty = std::min(e->tile[1], g.K);
     g.tz = std::min(e->tile[2], g.K);
@@ -373,6 +375,8 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY(dalloc(&e->d_pos, sizeof(double) * 3 * n));
     TRY(dalloc(&e->d_key, sizeof(int) * n));
     TRY(dalloc(&e->d_slot, sizeof(int) * n));
+    TRY(dalloc(&e->d_key3, sizeof(int) * n));
+    TRY(dalloc(&e->d_slot3, sizeof(int) * n));
     TRY(dalloc(&e->d_tperm, sizeof(int) * n));
     e->cols = (prm.terms & SPME_TERM_RECIP) && C >= 12 && spme::spread_cols_ok((int)K, 12, e->elem);
     if (e->cols) {
@@ -380,6 +384,8 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_scount, sizeof(int) * K3));
         TRY(dalloc(&e->d_soff, sizeof(int) * (K3 + 1)));
         TRY(dalloc(&e->d_sperm, sizeof(int) * n));
+        TRY(dalloc(&e->d_key2, sizeof(int) * n));
+        TRY(dalloc(&e->d_slot2, sizeof(int) * n));
         TRY(dalloc(&e->d_srec_idx, sizeof(int) * n));
         TRY(dalloc(&e->d_srec_start, sizeof(uint32_t) * n));
         TRY(dalloc(&e->d_srec_w, e->elem * record_width(e) * n));
@@ -526,7 +532,8 @@ void destroy_impl(spme_t *e) {
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
-                    e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2};
+                    e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2, e->d_key2,
+                    e->d_slot2,  e->d_key3,   e->d_slot3};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -550,9 +557,22 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
                                                       : cudaMemcpyDeviceToDevice,
                                  s));
     }
-    if (e->prm.terms & SPME_TERM_RECIP) {  // geometry and tile buffers set by the caller
-        TRY_CUDA(cudaMemsetAsync(e->d_tcount, 0, sizeof(int) * e->ntiles, s));
-        spme::launch_tile_keys(e->d_pos, n, e->g, e->d_key, e->d_tcount, e->d_slot, s);
+    const bool recip = (e->prm.terms & SPME_TERM_RECIP) != 0;  // geometry set by the caller
+    const bool real = (e->prm.terms & SPME_TERM_REAL) != 0;
+    const bool cols = recip && e->cols;
+    const int ncell = e->nc * e->nc * e->nc;
+    const int K3 = e->g.K * e->g.K * e->g.K;
+    if (recip) TRY_CUDA(cudaMemsetAsync(e->d_tcount, 0, sizeof(int) * e->ntiles, s));
+    if (cols) TRY_CUDA(cudaMemsetAsync(e->d_scount, 0, sizeof(int) * K3, s));
+    if (real) TRY_CUDA(cudaMemsetAsync(e->d_ccount, 0, sizeof(int) * ncell, s));
+    if (recip || real) {
+        // one pass over the positions for every key this engine sorts by
+        spme::launch_all_keys(e->d_pos, n, e->g, e->nc, e->d_key, recip ? e->d_tcount : nullptr,
+                              e->d_slot, e->d_key2, cols ? e->d_scount : nullptr, e->d_slot2,
+                              e->d_key3, real ? e->d_ccount : nullptr, e->d_slot3, s);
+        e->launches++;
+    }
+    if (recip) {
         spme::launch_scan(e->d_tcount, e->ntiles, e->d_toff, e->d_scan_tmp, s);
         spme::launch_scatter(e->d_key, e->d_slot, e->d_toff, n, e->d_tperm, s);
         if (is_fp32(e))
@@ -561,32 +581,25 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
         else
             spme::launch_records<double>(e->d_pos, e->d_tperm, n, e->g, e->d_rec_idx,
                                          e->d_rec_start, (double *)e->d_rec_w, s);
-        e->launches += 6;
-        if (e->cols) {
-            const int K3 = e->g.K * e->g.K * e->g.K;
-            TRY_CUDA(cudaMemsetAsync(e->d_scount, 0, sizeof(int) * K3, s));
-            spme::launch_start_keys(e->d_pos, n, e->g, e->d_key, e->d_scount, e->d_slot, s);
-            spme::launch_scan(e->d_scount, K3, e->d_soff, e->d_scan_tmp, s);
-            spme::launch_scatter(e->d_key, e->d_slot, e->d_soff, n, e->d_sperm, s);
-            if (is_fp32(e))
-                spme::launch_records<float>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
-                                            e->d_srec_start, (float *)e->d_srec_w, s);
-            else
-                spme::launch_records<double>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
-                                             e->d_srec_start, (double *)e->d_srec_w, s);
-            e->launches += 6;
-        }
+        e->launches += 5;
     }
-    if (e->prm.terms & SPME_TERM_REAL) {
-        int ncell = e->nc * e->nc * e->nc;
-        TRY_CUDA(cudaMemsetAsync(e->d_ccount, 0, sizeof(int) * ncell, s));
-        spme::launch_cell_keys(e->d_pos, n, e->prm.box_size, e->nc, e->d_key, e->d_ccount,
-                               e->d_slot, s);
+    if (cols) {
+        spme::launch_scan(e->d_scount, K3, e->d_soff, e->d_scan_tmp, s);
+        spme::launch_scatter(e->d_key2, e->d_slot2, e->d_soff, n, e->d_sperm, s);
+        if (is_fp32(e))
+            spme::launch_records<float>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
+                                        e->d_srec_start, (float *)e->d_srec_w, s);
+        else
+            spme::launch_records<double>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
+                                         e->d_srec_start, (double *)e->d_srec_w, s);
+        e->launches += 5;
+    }
+    if (real) {
         spme::launch_scan(e->d_ccount, ncell, e->d_coff, e->d_scan_tmp, s);
-        spme::launch_scatter(e->d_key, e->d_slot, e->d_coff, n, e->d_cperm, s);
+        spme::launch_scatter(e->d_key3, e->d_slot3, e->d_coff, n, e->d_cperm, s);
         spme::launch_cell_positions(e->d_pos, e->d_cperm, n, e->prm.box_size, e->nc, is_fp32(e),
                                     e->d_cpos, s);
-        e->launches += 6;
+        e->launches += 5;
     }
     TRY_CUDA(cudaGetLastError());
     return SPME_OK;

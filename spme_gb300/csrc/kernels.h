@@ -13,12 +13,13 @@
 namespace spme {
 
 // ---- P-build and counting sorts (pbuild.cu) -------------------------------
-// Tile key of each particle's stencil start, and a slot within its tile.
-void launch_tile_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
-                      int *slot, cudaStream_t s);
-// Stencil-start cell key ((sy K + sx) K + sz, K^3 keys) and slot within it.
-void launch_start_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
-                       int *slot, cudaStream_t s);
+// Sort keys with a slot within each key (atomic counts): the mesh tile of the
+// stencil start (key1), the stencil-start cell ((sy K + sx) K + sz, K^3 keys;
+// key2), the real-space cell (nc^3 cells of edge L/nc; key3), in one pass over
+// the positions.  A null count skips that key.
+void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
+                     int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
+                     int *slot3, cudaStream_t s);
 // Real-space cell key (nc^3 cells of edge L/nc) and slot within its cell.
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
                       int *slot, cudaStream_t s);

@@ -11,56 +11,59 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-__global__ void k_tile_keys(const double *__restrict__ pos, int n, MeshGeom g,
-                            int *__restrict__ key, int *__restrict__ count,
-                            int *__restrict__ slot) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int s[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        double fr;
-        mesh_coord(pos[3 * i + d], g.L, g.K, g.p, s[d], fr);
-    }
-    int k = ((s[2] / g.tz) * g.nty + s[1] / g.ty) * g.ntx + s[0] / g.tx;
-    key[i] = k;
-    slot[i] = atomicAdd(&count[k], 1);
-}
-
-// Key of the stencil-start cell in (y, x, z) order, z fastest: for a fixed
-// start column (sy, sx) the particles of a z range are contiguous.
-__global__ void k_start_keys(const double *__restrict__ pos, int n, MeshGeom g,
-                             int *__restrict__ key, int *__restrict__ count,
-                             int *__restrict__ slot) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int s[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        double fr;
-        mesh_coord(pos[3 * i + d], g.L, g.K, g.p, s[d], fr);
-    }
-    int k = (s[1] * g.K + s[0]) * g.K + s[2];
-    key[i] = k;
-    slot[i] = atomicAdd(&count[k], 1);
-}
-
 __global__ void k_cell_keys(const double *__restrict__ pos, int n, double L, int nc,
                             int *__restrict__ key, int *__restrict__ count,
                             int *__restrict__ slot) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double invL = 1.0 / L;
     int c[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        double x = pos[3 * i + d];
-        x -= L * floor(x / L);
-        int v = (int)(x / L * (double)nc);
-        c[d] = v >= nc ? nc - 1 : v;
+        double xw;
+        c[d] = cell_coord(pos[3 * i + d], L, invL, nc, xw);
     }
     int k = (c[2] * nc + c[1]) * nc + c[0];
     key[i] = k;
     slot[i] = atomicAdd(&count[k], 1);
+}
+
+// All sort keys of a position build in one pass over the positions: the mesh
+// tile of the stencil start (always), the stencil-start cell (key2, when
+// count2 is set) and the real-space cell (key3, when count3 is set), each with
+// its slot from an atomic count.
+__global__ void k_all_keys(const double *__restrict__ pos, int n, MeshGeom g, int nc,
+                           int *__restrict__ key1, int *__restrict__ count1,
+                           int *__restrict__ slot1, int *__restrict__ key2,
+                           int *__restrict__ count2, int *__restrict__ slot2,
+                           int *__restrict__ key3, int *__restrict__ count3,
+                           int *__restrict__ slot3) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s[3] = {0, 0, 0}, cc[3] = {0, 0, 0};
+    const bool mesh = count1 || count2;  // the mesh geometry is set only then
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const double x = pos[3 * i + d];
+        double fr, xw;
+        if (mesh) mesh_coord(x, g.L, g.invL, g.K, g.p, s[d], fr);
+        if (count3) cc[d] = cell_coord(x, g.L, g.invL, nc, xw);
+    }
+    if (count1) {
+        const int k = ((s[2] / g.tz) * g.nty + s[1] / g.ty) * g.ntx + s[0] / g.tx;
+        key1[i] = k;
+        slot1[i] = atomicAdd(&count1[k], 1);
+    }
+    if (count2) {
+        const int k = (s[1] * g.K + s[0]) * g.K + s[2];
+        key2[i] = k;
+        slot2[i] = atomicAdd(&count2[k], 1);
+    }
+    if (count3) {
+        const int k = (cc[2] * nc + cc[1]) * nc + cc[0];
+        key3[i] = k;
+        slot3[i] = atomicAdd(&count3[k], 1);
+    }
 }
 
 // Block-wide exclusive scan of one value per thread; returns the block total.
@@ -173,7 +176,7 @@ __global__ void k_records(const double *__restrict__ pos, const int *__restrict_
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         double fr;
-        mesh_coord(pos[3 * i + d], g.L, g.K, P, st[d], fr);
+        mesh_coord(pos[3 * i + d], g.L, g.invL, g.K, P, st[d], fr);
         bspline_weights<T, P>((T)fr, w[d]);
     }
     rec_idx[s] = i;
@@ -194,15 +197,13 @@ __global__ void k_cell_positions(const double *__restrict__ pos, const int *__re
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     int i = perm[s];
-    const double h = L / nc;
+    const double h = L / nc, invL = 1.0 / L;
     double o[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        double x = pos[3 * i + d];
-        x -= L * floor(x / L);
-        int c = (int)(x / L * (double)nc);
-        c = c >= nc ? nc - 1 : c;
-        o[d] = x - c * h;
+        double xw;
+        const int c = cell_coord(pos[3 * i + d], L, invL, nc, xw);
+        o[d] = xw - c * h;
     }
     G4 v;
     v.x = (G)o[0];
@@ -216,14 +217,12 @@ inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
 
-void launch_tile_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
-                      int *slot, cudaStream_t s) {
-    if (n > 0) k_tile_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, key, count, slot);
-}
-
-void launch_start_keys(const double *pos, int n, const MeshGeom &g, int *key, int *count,
-                       int *slot, cudaStream_t s) {
-    if (n > 0) k_start_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, key, count, slot);
+void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
+                     int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
+                     int *slot3, cudaStream_t s) {
+    if (n > 0)
+        k_all_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2, count2,
+                                                slot2, key3, count3, slot3);
 }
 
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
