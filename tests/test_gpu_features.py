@@ -170,3 +170,22 @@ def test_fused_mode_unavailable_for_unaligned_fp32_planes(gpu_lib):
     ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
     assert relerr(u, ref) < 1e-5
     eng.close()
+
+
+def test_overlap_mode_matches_serial(gpu_lib):
+    """Real-space sum on a second stream (overlap on) gives the same operator as
+    the default serial order, FP32 and FP64, with and without beta."""
+    n, L, K, p, R = 1500, 40.0, 32, 6, 4
+    pos, f = uniform_case(n, L, R, seed=11)
+    for prec, tol in (("fp64", 1e-14), ("fp32", 1e-6)):
+        out = {}
+        for ov in (0, 1):
+            eng = spme_gb300.Engine(n, L, 0.4, K, p, rcut=8.0, precision=prec, max_nrhs=R)
+            eng.set_overlap(ov)
+            eng.set_positions(pos)
+            u0 = np.ones((R, 3 * n), dtype=eng.dtype)
+            out[ov] = eng.apply(f.astype(eng.dtype), u0, alpha=0.7, beta=0.5)
+            eng.close()
+        assert relerr(out[1], out[0]) < tol
+    ref = oracle.full(pos, L, 0.4, 8.0, K, p, f, nthreads=4)
+    assert relerr((out[0] - 0.5) / 0.7, ref) < 1e-5
