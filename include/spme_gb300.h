@@ -123,12 +123,12 @@ long spme_launch_count(const spme_t *spme);
  * and the concurrent sum only slows them down). */
 int spme_set_overlap(spme_t *spme, int on);
 
-/* Spread kernel.  1 (default where it applies: K >= 32, at least 12
- * components, an engine created with max_nrhs >= 4): column gather, each mesh
+/* Spread kernel.  1 (default): column gather where it applies (K >= 32; in
+ * FP32 from 9 components on, below that the tile kernel is faster), each mesh
  * column visits only the particles whose stencil covers it, force components
- * across the lanes of a warp.  0: tile kernel, threads own the columns of a
- * mesh tile and visit every particle staged for the tile.  Mode 1 on an engine
- * without the column-gather buffers returns SPME_ERR_UNSUPPORTED. */
+ * across the lanes of a warp.  0: tile kernel always, threads own the columns
+ * of a mesh tile and visit every particle staged for the tile.  Mode 1 on an
+ * engine without the column-gather buffers returns SPME_ERR_UNSUPPORTED. */
 int spme_set_spread_mode(spme_t *spme, int mode);
 
 /* Transform strategy of the mesh pass.  1: cuFFT 2D (y, x) transforms of

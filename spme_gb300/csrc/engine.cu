@@ -378,7 +378,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY(dalloc(&e->d_key3, sizeof(int) * n));
     TRY(dalloc(&e->d_slot3, sizeof(int) * n));
     TRY(dalloc(&e->d_tperm, sizeof(int) * n));
-    e->cols = (prm.terms & SPME_TERM_RECIP) && C >= 12 && spme::spread_cols_ok((int)K, 12, e->elem);
+    e->cols = (prm.terms & SPME_TERM_RECIP) && spme::spread_cols_ok((int)K, (int)C, e->elem);
     if (e->cols) {
         const size_t K3 = K * K * K;
         TRY(dalloc(&e->d_scount, sizeof(int) * K3));
@@ -667,7 +667,12 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         if (!e->d_mesh || !e->d_cmesh || !e->d_tab) return SPME_ERR_STATE;
         PlanPair *pp;
         TRY(get_plans(e, C, &pp));
-        if (e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem)) {
+        // column gather where it applies; measured on GB300 (K = 256, N = 1e6): in FP64
+        // it wins at every C (8.0 vs 19.6 ms at C = 3), in FP32 from C = 9 on (the
+        // tile kernel's per-component cost is lower at C = 3, 6)
+        const bool use_cols = e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem) &&
+                              (e->elem == 8 || C >= 9);
+        if (use_cols) {
             spme::launch_gather_rows<T>(F, e->d_srec_idx, n, C, (T *)e->d_Fs, s);
             TRY_CUDA(spme::launch_spread_cols<T>(e->d_soff, e->d_srec_start,
                                                  (const T *)e->d_srec_w, (const T *)e->d_Fs, C,

@@ -284,10 +284,11 @@ cudaError_t dispatch_cpl(const int *soff, const uint32_t *rec_start, const T *re
 
 // The z runs of one tile must not wrap onto themselves (TZ + p - 1 <= K) and
 // the p + 1 start columns of a column pair must be distinct: K >= 32 covers
-// both for p <= 8.  Below 12 components most lanes would idle.
+// both for p <= 8.  Any number of components (the cost is per visit: below 16
+// components lanes idle, but the tile kernel's wasted visits cost more).
 bool spread_cols_ok(int K, int C, size_t elem) {
     (void)elem;
-    return K >= 32 && K <= 1024 && C >= 12;
+    return K >= 32 && K <= 1024 && C >= 1;
 }
 
 template <typename T>

@@ -179,6 +179,7 @@ def test_device_pointer_api(gpu_lib):
 
 # (N, L, K, p, R): even / odd K, all orders, one and two component chunks
 SPREAD_CASES = [
+    (800, 40.0, 40, 6, 1),
     (900, 40.0, 32, 6, 4),
     (1200, 50.0, 45, 4, 5),
     (700, 36.0, 36, 8, 16),
