@@ -128,18 +128,26 @@ __device__ __forceinline__ void dft_small(const Cx<T> (&v)[R], Cx<T> (&o)[R]) {
 // b L3 + j + q1 L + q2 L R1 (L3 = L R1 R2); the R2 stage sees span L R1 and
 // offset j + q1 L.  DIT runs the R1 stage first, DIF the R2 stage first.  A
 // pass with L = 1 has j = 0: its R1-stage twiddles are 1 and are skipped.
-template <typename T, int W, int CT, int R1, int R2, bool DIF>
-__device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int K, int L,
+// KC, LC: K and L as compile-time constants (0: taken from the arguments).
+template <typename T, int W, int CT, int R1, int R2, bool DIF, int KC = 0, int LC = 0>
+__device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int Kr, int Lr,
                                       const Cx<T> *__restrict__ tw, int bi0) {
     constexpr int BS = CT / (3 * W);
+    const int K = KC ? KC : Kr, L = LC ? LC : Lr;
     const int La = L * R1, L3 = La * R2;
     const int nb = K / (R1 * R2), ts1 = K / La, ts2 = K / L3;
     const bool unit1 = L == 1;
     DivMod dl;
-    dl.init(L);
+    if constexpr (LC == 0) dl.init(L);
+#pragma unroll(KC ? 4 : 1)
     for (int bi = bi0; bi < nb; bi += BS) {
-        int j;
-        const int b = dl.div(bi, j);
+        int j, b;
+        if constexpr (LC != 0) {
+            b = bi / LC;  // compile-time divisor
+            j = bi - b * LC;
+        } else {
+            b = dl.div(bi, j);
+        }
         Cx<T> *x = sb + (size_t)(b * L3 + j) * W;
         Cx<T> v[R2][R1];
 #pragma unroll
@@ -293,7 +301,37 @@ constexpr ZCfg kCfg64[] = {{8, 384, 1, 6}, {4, 192, 2, 12}, {8, 192, 1, 12},
 // (chunk starts are multiples of W: 16-byte aligned in the global layout), all
 // 3R components.  Threads 0..CT-1 transform; the warp after them moves data: TMA loads into
 // the two buffers, TMA stores of finished buffers.
-template <typename T, int W, int CT, int MINB, int MAXP>
+// Pass sequence of the z transform: generic (from the plan) or, for KS = 256,
+// the two radix-16 passes with compile-time spans.
+template <typename T, int W, int CT, int KS, bool DIF>
+__device__ __forceinline__ void zpasses(Cx<T> *cb, const ZPlan &zp, const Cx<T> *tw, int bi0) {
+    if constexpr (KS == 256) {
+        if constexpr (DIF) {
+            zpass<T, W, CT, 4, 4, true, 256, 16>(cb, 256, 16, tw, bi0);
+            compute_sync<CT>();
+            zpass<T, W, CT, 4, 4, true, 256, 1>(cb, 256, 1, tw, bi0);
+            compute_sync<CT>();
+        } else {
+            zpass<T, W, CT, 4, 4, false, 256, 1>(cb, 256, 1, tw, bi0);
+            compute_sync<CT>();
+            zpass<T, W, CT, 4, 4, false, 256, 16>(cb, 256, 16, tw, bi0);
+        }
+    } else {
+        if constexpr (DIF) {
+            for (int i = zp.npass - 1; i >= 0; i--) {
+                zstage<T, W, CT, true>(cb, zp.K, zp.pcode[i], zp.pspan[i], tw, bi0);
+                compute_sync<CT>();
+            }
+        } else {
+            for (int i = 0; i < zp.npass; i++) {
+                zstage<T, W, CT, false>(cb, zp.K, zp.pcode[i], zp.pspan[i], tw, bi0);
+                if (i + 1 < zp.npass) compute_sync<CT>();
+            }
+        }
+    }
+}
+
+template <typename T, int W, int CT, int MINB, int MAXP, int KS>
 __global__ void __launch_bounds__(CT + 32, MINB)
 k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__ tab2,
                  const Cx<T> *__restrict__ tw_g, const int *__restrict__ perm_g,
@@ -409,10 +447,7 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__
         Cx<T> *B = b ? buf1 : buf0;
         Cx<T> *cb = B + (size_t)gcol * GS + wcol;
         // forward DIF, passes from the last down
-        for (int i = zp.npass - 1; i >= 0; i--) {
-            zstage<T, W, CT, true>(cb, K, zp.pcode[i], zp.pspan[i], tw, bi0);
-            compute_sync<CT>();
-        }
+        zpasses<T, W, CT, KS, true>(cb, zp, tw, bi0);
         // influence, digit-reversed z order
 #pragma unroll
         for (int i = 0; i < MAXP; i++) {
@@ -434,10 +469,7 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__
         }
         compute_sync<CT>();
         // inverse DIT, passes from the first up
-        for (int i = 0; i < zp.npass; i++) {
-            zstage<T, W, CT, false>(cb, K, zp.pcode[i], zp.pspan[i], tw, bi0);
-            if (i + 1 < zp.npass) compute_sync<CT>();
-        }
+        zpasses<T, W, CT, KS, false>(cb, zp, tw, bi0);
         // hand the buffer to the TMA warp (its store reads what this thread wrote)
         fence_proxy_async();
         mbar_arrive(&done[b]);
@@ -595,7 +627,12 @@ bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem) {
 template <typename T, int W, int CT, int MINB, int MAXP>
 cudaError_t launch_zcfg(const CUtensorMap &map, const T *tab2, const T *tw, const int *perm,
                         const ZPlan &zp, T twopi_L, int R, int zb, int *err, cudaStream_t s) {
-    auto kern = k_zfft_influence<T, W, CT, MINB, MAXP>;
+    // K = 256 with its usual plan (radix-16 passes of spans 1 and 16): the
+    // compile-time pass sequence
+    const bool k256 = zp.K == 256 && zp.npass == 2 && zp.pcode[0] == 44 && zp.pcode[1] == 44 &&
+                      zp.pspan[0] == 1 && zp.pspan[1] == 16;
+    auto kern = k256 ? k_zfft_influence<T, W, CT, MINB, MAXP, 256>
+                     : k_zfft_influence<T, W, CT, MINB, MAXP, 0>;
     const int K = zp.K, Kh = K / 2 + 1;
     const size_t smem = zsmem_bytes<T>(K, W);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

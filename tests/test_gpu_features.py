@@ -189,3 +189,20 @@ def test_overlap_mode_matches_serial(gpu_lib):
         assert relerr(out[1], out[0]) < tol
     ref = oracle.full(pos, L, 0.4, 8.0, K, p, f, nthreads=4)
     assert relerr((out[0] - 0.5) / 0.7, ref) < 1e-5
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp64", 1e-13)])
+def test_fused_zfft_k256_matches_3d_fft(gpu_lib, prec, tol):
+    """K = 256 runs the compile-time pass sequence of the fused kernel; it must
+    agree with cuFFT's 3D path (validated against the oracle at other K)."""
+    n, L, K, p, R = 3000, 256.0, 256, 6, 3
+    pos, f = uniform_case(n, L, R, seed=256)
+    out = {}
+    for mode in (0, 1):
+        eng = spme_gb300.Engine(n, L, 0.4, K, p, precision=prec, max_nrhs=R,
+                                terms=spme_gb300.TERM_RECIP)
+        eng.set_fft_mode(mode)
+        eng.set_positions(pos)
+        out[mode] = eng.apply(f.astype(eng.dtype))
+        eng.close()
+    assert relerr(out[1], out[0]) < tol
