@@ -69,8 +69,10 @@ constexpr int kCap = 512;  // candidates staged in shared memory per cell
 // Sums over one batch run in T; batches are accumulated in FP64.  No block
 // barrier after the staging.  More than kCap candidates (very dense cells)
 // take a second path that reads candidates straight from global memory.
+// FP32: 64 registers, 16 blocks (32 warps) per SM (measured faster than the
+// unconstrained 80 registers); FP64 needs more registers.
 template <typename T, typename G>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 16 : 8)
 k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ cell_perm,
             const typename Geo4<G>::type *__restrict__ cpos, const T *__restrict__ F, int R,
             G L, G h, G rc2, T xi, T a, T self_c, int with_self, T *__restrict__ W) {
