@@ -206,3 +206,24 @@ def test_fused_zfft_k256_matches_3d_fft(gpu_lib, prec, tol):
         out[mode] = eng.apply(f.astype(eng.dtype))
         eng.close()
     assert relerr(out[1], out[0]) < tol
+
+
+@pytest.mark.parametrize("K,prec,tol", [(320, "fp32", 2e-6), (512, "fp32", 2e-6), (384, "fp64", 1e-13)])
+def test_fused_zfft_large_k_matches_3d_fft(gpu_lib, K, prec, tol):
+    """K > 256: the fused kernel moves each z column as several TMA boxes
+    (z chunks of K/2 or K/4 rows); it must agree with cuFFT's 3D path."""
+    n, L, p, R = 2000, float(K), 4, 2
+    pos, f = uniform_case(n, L, R, seed=K)
+    out = {}
+    for mode in (0, 1):
+        eng = spme_gb300.Engine(n, L, 0.5, K, p, precision=prec, max_nrhs=R,
+                                terms=spme_gb300.TERM_RECIP)
+        try:
+            eng.set_fft_mode(mode)
+        except spme_gb300.SpmeError:
+            eng.close()
+            pytest.skip(f"K={K} {prec}: no fused configuration")
+        eng.set_positions(pos)
+        out[mode] = eng.apply(f.astype(eng.dtype))
+        eng.close()
+    assert relerr(out[1], out[0]) < tol
