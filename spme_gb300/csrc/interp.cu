@@ -6,9 +6,10 @@
 // [CG][HZB][HYB][HX] (HX = 24 wide: every lane's x offset fits, and the
 // component-plane stride is 24 (mod 32) words so the gather below is
 // bank-conflict free):
-//   * interior tiles: one TMA (cp.async.bulk.tensor) load per chunk,
-//     completing on an mbarrier (bounded wait, error flag on timeout);
-//   * tiles whose halo wraps the periodic boundary: 16-byte vector loads.
+//   * one TMA (cp.async.bulk.tensor) load per chunk, completing on an mbarrier
+//     (bounded wait, error flag on timeout); for tiles whose halo wraps the
+//     periodic boundary the part past K arrives as zeros and is patched with
+//     16-byte vector loads (all rows with plain loads when TMA is unavailable).
 // Each warp then interpolates the tile's own particles (sorted by stencil
 // start) from shared memory: lanes are (x offset 0..7, component 0..3)
 // pairs, the x offsets summed with shuffles.  Every particle is handled by
@@ -56,10 +57,12 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
     const int hx = min(g.tx, K - ox) + P - 1;
     const int hy = min(g.ty, K - oy) + P - 1;
     const int hz = min(g.tz, K - oz) + P - 1;
-    // TMA: halo must not wrap, and the box's innermost start coordinate times the
-    // element size must be a multiple of 16 bytes
-    const bool tma = use_tma && ox + hx <= K && oy + hy <= K && oz + hz <= K &&
-                     ((size_t)ox * sizeof(T)) % 16 == 0;
+    // TMA: the box's innermost start coordinate times the element size must be a
+    // multiple of 16 bytes.  A halo that wraps the periodic boundary is loaded by
+    // TMA too (the part past K arrives as zeros) and the wrapped part patched
+    // with plain loads.
+    const bool wraps = ox + hx > K || oy + hy > K || oz + hz > K;
+    const bool tma = use_tma && ((size_t)ox * sizeof(T)) % 16 == 0;
     const size_t K2 = (size_t)K * K, K3 = K2 * K;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int xs = lane >> 2, cl = lane & 3;
@@ -69,6 +72,39 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
         mbar_fence_init();
     }
     __syncthreads();
+
+    // rows [c][z][y][0..kHX) of the halo region with plain (wrap-aware) loads:
+    // all of them, or only the elements past the periodic boundary
+    auto stage_rows = [&](int c0, int nc, bool only_wrapped) {
+        const bool vec = (K % VW) == 0 && (ox % VW) == 0;
+        DivMod dnv, dhy, dhz;
+        dnv.init(NV);
+        dhy.init(hy);
+        dhz.init(hz);
+        const int nrow = nc * hz * hy;
+        for (int q = threadIdx.x; q < nrow * NV; q += kThreads) {
+            int v, y, z;
+            const int row = dnv.div(q, v);
+            const int cz = dhy.div(row, y);
+            const int c = dhz.div(cz, z);
+            int gy = oy + y, gz = oz + z;
+            const bool row_wraps = gy >= K || gz >= K;
+            gy -= gy >= K ? K : 0;
+            gz -= gz >= K ? K : 0;
+            const int x0 = ox + v * VW;
+            if (only_wrapped && !row_wraps && (x0 + VW <= K || v * VW >= hx)) continue;
+            const T *src = mesh + (size_t)(c0 + c) * K3 + (size_t)gz * K2 + (size_t)gy * K;
+            T *dst = box + (size_t)c * PS + (z * HYB + y) * kHX + v * VW;
+            if (vec) {
+                *reinterpret_cast<V *>(dst) = __ldg(reinterpret_cast<const V *>(src + x0 % K));
+            } else {
+#pragma unroll
+                for (int e = 0; e < VW; e++)
+                    if (!only_wrapped || row_wraps || x0 + e >= K) dst[e] = __ldg(src + (x0 + e) % K);
+            }
+        }
+        __syncthreads();
+    };
 
     int chunk = 0;
     for (int c0 = 0; c0 < C; c0 += CG, chunk++) {
@@ -84,33 +120,9 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
                 if (threadIdx.x == 0) atomicExch(err, 1);
                 return;
             }
+            if (wraps) stage_rows(c0, nc, true);
         } else {
-            // rows [c][z][y][0..kHX) of the halo region, wrap-aware
-            const bool vec = (K % VW) == 0 && (ox % VW) == 0;
-            DivMod dnv, dhy, dhz;
-            dnv.init(NV);
-            dhy.init(hy);
-            dhz.init(hz);
-            const int nrow = nc * hz * hy;
-            for (int q = threadIdx.x; q < nrow * NV; q += kThreads) {
-                int v, y, z;
-                const int row = dnv.div(q, v);
-                const int cz = dhy.div(row, y);
-                const int c = dhz.div(cz, z);
-                int gy = oy + y, gz = oz + z;
-                gy -= gy >= K ? K : 0;
-                gz -= gz >= K ? K : 0;
-                const T *src = mesh + (size_t)(c0 + c) * K3 + (size_t)gz * K2 + (size_t)gy * K;
-                T *dst = box + (size_t)c * PS + (z * HYB + y) * kHX + v * VW;
-                const int x0 = ox + v * VW;
-                if (vec) {
-                    *reinterpret_cast<V *>(dst) = __ldg(reinterpret_cast<const V *>(src + x0 % K));
-                } else {
-#pragma unroll
-                    for (int e = 0; e < VW; e++) dst[e] = __ldg(src + (x0 + e) % K);
-                }
-            }
-            __syncthreads();
+            stage_rows(c0, nc, false);
         }
         // the next particle's record is loaded while this one is interpolated
         constexpr int kWarps = kThreads / 32;
