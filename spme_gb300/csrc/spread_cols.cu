@@ -184,10 +184,29 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 ws.dz_row[lane] = make_int2(sz - (partB ? z0 + K : z0), s);  // dz in [-(P-1), ext)
                 T wz[P];
                 load_weights<T, P>(rw + 2 * P, wz);
+                // 16-byte stores (scalar stores at this lane stride conflict 16-way)
+                constexpr int PW = WarpScratch<T, P>::PW, VW = 16 / (int)sizeof(T);
+                using V = typename V16<T>::type;
 #pragma unroll
-                for (int j = 0; j < WarpScratch<T, P>::PW; j++) {
-                    ws.wt[lane][0][j] = j < P ? w0 * wz[j] : T(0);
-                    ws.wt[lane][1][j] = j < P ? w1 * wz[j] : T(0);
+                for (int h = 0; h < 2; h++) {
+                    const T w = h ? w1 : w0;
+                    T row[PW];
+#pragma unroll
+                    for (int j = 0; j < PW; j++) row[j] = j < P ? w * wz[j] : T(0);
+#pragma unroll
+                    for (int v = 0; v < PW / VW; v++) {
+                        V q;
+                        if constexpr (VW == 4) {
+                            q.x = row[4 * v];
+                            q.y = row[4 * v + 1];
+                            q.z = row[4 * v + 2];
+                            q.w = row[4 * v + 3];
+                        } else {
+                            q.x = row[2 * v];
+                            q.y = row[2 * v + 1];
+                        }
+                        reinterpret_cast<V *>(&ws.wt[lane][h][0])[v] = q;
+                    }
                 }
             }
             __syncwarp();
