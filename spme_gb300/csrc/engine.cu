@@ -92,6 +92,8 @@ struct _spme_t {
     void *d_Fs = nullptr;  // force rows in start-cell order
     int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
     void *d_cpos = nullptr;  // float4 (FP32 engine) or double4 (FP64 engine)
+    void *d_pair = nullptr;  // Chebyshev table of the pair functions (FP64 engines)
+    spme::PairTable pair;
     void *d_mesh = nullptr, *d_cmesh = nullptr, *d_tab = nullptr;
     double *d_bmod2 = nullptr;
     void *d_work = nullptr;
@@ -401,6 +403,16 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_coff, sizeof(int) * (ncell + 1)));
         TRY(dalloc(&e->d_cperm, sizeof(int) * n));
         TRY(dalloc(&e->d_cpos, sizeof(double4) * n));
+        // FP64: the pair functions from a Chebyshev table instead of erfc / exp
+        std::vector<double> coef;
+        if (!is_fp32(e) && spme::build_pair_table(prm.xi, prm.radius, prm.rcut, &coef, &e->pair)) {
+            TRY(dalloc(&e->d_pair, sizeof(double) * coef.size()));
+            TRY_CUDA(cudaMemcpy(e->d_pair, coef.data(), sizeof(double) * coef.size(),
+                                cudaMemcpyHostToDevice));
+            e->pair.coef = (const double *)e->d_pair;
+        } else {
+            e->pair = spme::PairTable{};
+        }
     }
     if (prm.terms & SPME_TERM_RECIP) {
         TRY(dalloc(&e->d_mesh, e->elem * K * K * K * C));
@@ -532,7 +544,7 @@ void destroy_impl(spme_t *e) {
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
-                    e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2, e->d_key2,
+                    e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2, e->d_pair, e->d_key2,
                     e->d_slot2,  e->d_key3,   e->d_slot3};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
@@ -654,7 +666,7 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
             TRY_CUDA(spme::launch_realspace<T>(e->nc, e->d_coff, e->d_cperm, e->d_cpos, F, R,
                                                e->prm.box_size, e->prm.rcut, e->prm.xi,
                                                e->prm.radius, (terms & SPME_TERM_SELF) ? 1 : 0,
-                                               W, rss));
+                                               e->pair, W, rss));
         } else {
             spme::launch_self<T>(F, n, R, self_coeff(e->prm.xi, e->prm.radius), W, rss);
         }

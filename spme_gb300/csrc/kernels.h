@@ -109,6 +109,23 @@ template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
                              const T *F, int R, double L, double rc, double xi, double a,
                              int with_self, T *W, cudaStream_t s);
+// Piecewise Chebyshev table of the real-space pair functions F(r), G(r) for FP64
+// engines (xi and a fixed per engine): degree kPairDeg on nseg1 segments of
+// [r_lo, r_mid) and nseg2 of [r_mid, r_hi]; coef (device) holds the F and G
+// coefficients interleaved per segment.  A null coef means no table.
+constexpr int kPairDeg = 10;
+struct PairTable {
+    const double *coef = nullptr;
+    double r_lo = 0, r_mid = 0, r_hi = 0, inv_h1 = 0, inv_h2 = 0;
+    int nseg1 = 0, nseg2 = 0;
+};
+// Fits the table on the host (checked between nodes to 2e-13 relative);
+// false if no fit meets that within 4096 segments.
+bool build_pair_table(double xi, double a, double rc, std::vector<double> *coef, PairTable *t);
+template <typename T>
+cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
+                             const T *F, int R, double L, double rc, double xi, double a,
+                             int with_self, const PairTable &tab, T *W, cudaStream_t s);
 
 // ---- layout conversions (pack.cu) -----------------------------------------
 // W = self_c * F (the self term alone, when no real-space sum is requested)

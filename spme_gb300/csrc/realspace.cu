@@ -7,6 +7,10 @@
 //
 // One CTA per cell of edge >= rc; a warp per particle of the cell against the
 // candidates of the 27 neighbour cells (details at the kernel below).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "kernels.h"
 
 namespace spme {
@@ -42,6 +46,42 @@ __device__ __forceinline__ void real_FG(T r, T xi, T a, T &F, T &G) {
     G = g / a;
 }
 
+// F and G from the per-engine Chebyshev table (FP64 engines): false when r is
+// outside the table (the caller then evaluates real_FG directly).  Clenshaw
+// recurrence in t in [-1, 1] on the segment holding r; F and G coefficients
+// interleaved.
+__device__ __forceinline__ bool table_FG(const PairTable &tb, double r, double &F, double &G) {
+    if (!tb.coef || r < tb.r_lo || r > tb.r_hi) return false;
+    int seg;
+    double u;
+    if (r < tb.r_mid) {
+        u = (r - tb.r_lo) * tb.inv_h1;
+        seg = min((int)u, tb.nseg1 - 1);
+        u -= seg;
+    } else {
+        u = (r - tb.r_mid) * tb.inv_h2;
+        const int s2 = min((int)u, tb.nseg2 - 1);
+        u -= s2;
+        seg = tb.nseg1 + s2;
+    }
+    const double t = 2.0 * u - 1.0;
+    const double2 *c = reinterpret_cast<const double2 *>(tb.coef) + (size_t)seg * (kPairDeg + 1);
+    double bF = 0.0, bF1 = 0.0, bG = 0.0, bG1 = 0.0;
+#pragma unroll
+    for (int k = kPairDeg; k >= 1; k--) {
+        const double2 ck = __ldg(c + k);
+        const double nF = 2.0 * t * bF - bF1 + ck.x, nG = 2.0 * t * bG - bG1 + ck.y;
+        bF1 = bF;
+        bG1 = bG;
+        bF = nF;
+        bG = nG;
+    }
+    const double2 c0 = __ldg(c);
+    F = t * bF - bF1 + 0.5 * c0.x;
+    G = t * bG - bG1 + 0.5 * c0.y;
+    return true;
+}
+
 template <typename G> struct Geo4;
 template <> struct Geo4<float> { using type = float4; };
 template <> struct Geo4<double> { using type = double4; };
@@ -75,7 +115,8 @@ template <typename T, typename G>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 16 : 8)
 k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ cell_perm,
             const typename Geo4<G>::type *__restrict__ cpos, const T *__restrict__ F, int R,
-            G L, G h, G rc2, T xi, T a, T self_c, int with_self, T *__restrict__ W) {
+            G L, G h, G rc2, T xi, T a, T self_c, int with_self, PairTable tab,
+            T *__restrict__ W) {
     __shared__ int nb_beg[27], nb_pre[28], nnb;
     __shared__ G nb_shift[27][3];
     __shared__ G cx[kCap], cy[kCap], cz[kCap];
@@ -171,7 +212,14 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
                     }
                     const G rr = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
                     T Fv, Gv;
-                    real_FG<T>((T)rr, xi, a, Fv, Gv);
+                    bool done = false;
+                    if constexpr (sizeof(T) == 8) {
+                        double Fd, Gd;
+                        done = table_FG(tab, (double)rr, Fd, Gd);
+                        Fv = (T)Fd;
+                        Gv = (T)Gd;
+                    }
+                    if (!done) real_FG<T>((T)rr, xi, a, Fv, Gv);
                     const G ir = G(1) / rr;
                     pF[warp][lane] = Fv;
                     pG[warp][lane] = Gv;
@@ -261,7 +309,7 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
 template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
                              const T *F, int R, double L, double rc, double xi, double a,
-                             int with_self, T *W, cudaStream_t s) {
+                             int with_self, const PairTable &tab, T *W, cudaStream_t s) {
     const double rsp = 0.56418958354775628695;
     const double self_c = (1.0 - 6.0 * xi * a * rsp + 40.0 / 3.0 * xi * xi * xi * a * a * a * rsp) / a;
     const int ncell = nc * nc * nc;
@@ -269,12 +317,122 @@ cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, 
     if constexpr (sizeof(T) == 8)
         k_realspace<T, double><<<ncell, kThreads, 0, s>>>(
             nc, cell_off, cell_perm, (const double4 *)cpos, F, R, L, h, rc * rc, (T)xi, (T)a,
-            (T)self_c, with_self, W);
+            (T)self_c, with_self, tab, W);
     else
         k_realspace<T, float><<<ncell, kThreads, 0, s>>>(
             nc, cell_off, cell_perm, (const float4 *)cpos, F, R, (float)L, (float)h,
-            (float)(rc * rc), (T)xi, (T)a, (T)self_c, with_self, W);
+            (float)(rc * rc), (T)xi, (T)a, (T)self_c, with_self, tab, W);
     return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
+                             const T *F, int R, double L, double rc, double xi, double a,
+                             int with_self, T *W, cudaStream_t s) {
+    return launch_realspace<T>(nc, cell_off, cell_perm, cpos, F, R, L, rc, xi, a, with_self,
+                               PairTable{}, W, s);
+}
+
+namespace {
+
+// real_FG on the host (same formula, std::erfc / std::exp in FP64).
+void host_real_FG(double r, double xi, double a, double &F, double &G) {
+    const double rsp = 0.56418958354775628695;
+    const double xr = xi * r, e = std::exp(-xr * xr), ec = std::erfc(xr);
+    const double r2 = r * r, a3 = a * a * a, ir = 1.0 / r, ir3 = ir * ir * ir, ir2 = ir * ir;
+    const double xi2 = xi * xi, xi3 = xi2 * xi, xi5 = xi3 * xi2, xi7 = xi5 * xi2;
+    double f = ec * (0.75 * a * ir + 0.5 * a3 * ir3) +
+               e * rsp * (4.0 * xi7 * a3 * r2 * r2 + 3.0 * xi3 * a * r2 - 20.0 * xi5 * a3 * r2 -
+                          4.5 * xi * a + 14.0 * xi3 * a3 + xi * a3 * ir2);
+    double g = ec * (0.75 * a * ir - 1.5 * a3 * ir3) +
+               e * rsp * (-4.0 * xi7 * a3 * r2 * r2 - 3.0 * xi3 * a * r2 + 16.0 * xi5 * a3 * r2 +
+                          1.5 * xi * a - 2.0 * xi3 * a3 - 3.0 * xi * a3 * ir2);
+    if (r < 2.0 * a) {
+        f += (1.0 - 9.0 * r / (32.0 * a)) - (0.75 * a * ir + 0.5 * a3 * ir3);
+        g += (3.0 * r / (32.0 * a)) - (0.75 * a * ir - 1.5 * a3 * ir3);
+    }
+    F = f / a;
+    G = g / a;
+}
+
+// Chebyshev coefficients (degree kPairDeg) of F and G on [x0, x0 + h],
+// interleaved, from the values at the kPairDeg + 1 Chebyshev nodes.
+void fit_segment(double x0, double h, double xi, double a, double *out) {
+    constexpr int n = kPairDeg + 1;
+    double fv[n], gv[n];
+    for (int j = 0; j < n; j++) {
+        const double th = M_PI * (j + 0.5) / n;
+        host_real_FG(x0 + 0.5 * h * (std::cos(th) + 1.0), xi, a, fv[j], gv[j]);
+    }
+    for (int k = 0; k < n; k++) {
+        double sf = 0.0, sg = 0.0;
+        for (int j = 0; j < n; j++) {
+            const double c = std::cos(M_PI * k * (j + 0.5) / n);
+            sf += fv[j] * c;
+            sg += gv[j] * c;
+        }
+        out[2 * k] = 2.0 * sf / n;
+        out[2 * k + 1] = 2.0 * sg / n;
+    }
+}
+
+double eval_segment(const double *c, double t, int which) {
+    double b = 0.0, b1 = 0.0;
+    for (int k = kPairDeg; k >= 1; k--) {
+        const double nb = 2.0 * t * b - b1 + c[2 * k + which];
+        b1 = b;
+        b = nb;
+    }
+    return t * b - b1 + 0.5 * c[which];
+}
+
+}  // namespace
+
+bool build_pair_table(double xi, double a, double rc, std::vector<double> *coef, PairTable *t) {
+    // [r_lo, r_mid): overlap form (r < 2a); [r_mid, rc]: far form.  Below r_lo
+    // = a/2 the closed form's cancelling 1/r^2 terms leave rounding noise above
+    // 1e-13 relative that no fit reproduces: those (rare) pairs are evaluated
+    // directly.
+    const double r_lo = 0.5 * a, r_mid = std::min(2.0 * a, rc);
+    if (rc <= r_lo) return false;
+    double hmax = 0.1 * std::min(a, 1.0 / xi);
+    for (int attempt = 0; attempt < 4; attempt++, hmax *= 0.5) {
+        const int n1 = std::max(1, (int)std::ceil((r_mid - r_lo) / hmax));
+        const int n2 = rc > r_mid ? std::max(1, (int)std::ceil((rc - r_mid) / hmax)) : 0;
+        if (n1 + n2 > 4096) break;
+        const double h1 = (r_mid - r_lo) / n1, h2 = n2 ? (rc - r_mid) / n2 : 1.0;
+        coef->assign((size_t)(n1 + n2) * (kPairDeg + 1) * 2, 0.0);
+        for (int s = 0; s < n1 + n2; s++) {
+            const double x0 = s < n1 ? r_lo + s * h1 : r_mid + (s - n1) * h2;
+            fit_segment(x0, s < n1 ? h1 : h2, xi, a, coef->data() + (size_t)s * (kPairDeg + 1) * 2);
+        }
+        // the fit between the nodes, relative to the function scale there
+        bool ok = true;
+        for (int s = 0; s < n1 + n2 && ok; s++) {
+            const double x0 = s < n1 ? r_lo + s * h1 : r_mid + (s - n1) * h2;
+            const double hh = s < n1 ? h1 : h2;
+            const double *c = coef->data() + (size_t)s * (kPairDeg + 1) * 2;
+            for (int q = 0; q <= 16 && ok; q++) {
+                const double tt = -1.0 + q / 8.0;
+                double F, G;
+                host_real_FG(x0 + 0.5 * hh * (tt + 1.0), xi, a, F, G);
+                const double scale = std::fabs(F) + std::fabs(G) + 1e-300;
+                ok = std::fabs(eval_segment(c, tt, 0) - F) <= 2e-13 * scale &&
+                     std::fabs(eval_segment(c, tt, 1) - G) <= 2e-13 * scale;
+            }
+        }
+        if (!ok) continue;
+        t->coef = nullptr;  // the caller points it at the device copy
+        t->r_lo = r_lo;
+        t->r_mid = r_mid;
+        t->r_hi = rc;
+        t->inv_h1 = 1.0 / h1;
+        t->inv_h2 = 1.0 / h2;
+        t->nseg1 = n1;
+        t->nseg2 = n2;
+        return true;
+    }
+    return false;
 }
 
 template cudaError_t launch_realspace<float>(int, const int *, const int *, const void *,
@@ -283,5 +441,12 @@ template cudaError_t launch_realspace<float>(int, const int *, const int *, cons
 template cudaError_t launch_realspace<double>(int, const int *, const int *, const void *,
                                               const double *, int, double, double, double,
                                               double, int, double *, cudaStream_t);
+template cudaError_t launch_realspace<float>(int, const int *, const int *, const void *,
+                                             const float *, int, double, double, double, double,
+                                             int, const PairTable &, float *, cudaStream_t);
+template cudaError_t launch_realspace<double>(int, const int *, const int *, const void *,
+                                              const double *, int, double, double, double,
+                                              double, int, const PairTable &, double *,
+                                              cudaStream_t);
 
 }  // namespace spme
