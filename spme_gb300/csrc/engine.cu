@@ -57,6 +57,10 @@ struct _spme_t {
     int last_error = SPME_OK;
     cudaStream_t own_stream = nullptr, stream = nullptr, aux = nullptr;
     cudaStream_t cap_stream = nullptr;  // graph capture when the caller's stream is the legacy default
+    // host-pointer applies: inputs copied on their own stream (overlapping work
+    // already queued on the main stream, e.g. a position build)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_staged = nullptr, ev_stage_free = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int profiling = 0;  // 1: stage events; 2: events + real-space serialized
     cudaEvent_t ev[kStages + 1] = {};
@@ -365,6 +369,9 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
     TRY_CUDA(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking));
     TRY_CUDA(cudaStreamCreateWithFlags(&e->cap_stream, cudaStreamNonBlocking));
+    TRY_CUDA(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
+    TRY_CUDA(cudaEventCreateWithFlags(&e->ev_staged, cudaEventDisableTiming));
+    TRY_CUDA(cudaEventCreateWithFlags(&e->ev_stage_free, cudaEventDisableTiming));
     e->stream = e->own_stream;
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
@@ -555,6 +562,9 @@ void destroy_impl(spme_t *e) {
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->aux) cudaStreamDestroy(e->aux);
     if (e->cap_stream) cudaStreamDestroy(e->cap_stream);
+    if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
+    if (e->ev_staged) cudaEventDestroy(e->ev_staged);
+    if (e->ev_stage_free) cudaEventDestroy(e->ev_stage_free);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
     delete e;
 }
@@ -821,15 +831,21 @@ int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
         char *up = (char *)u + el * (size_t)r0 * ldu;
         int st;
         if (mem == SPME_MEM_HOST) {
+            // stage the inputs on the copy stream (after the staging buffers' last
+            // use), so the copy overlaps what the main stream is still running
+            TRY_CUDA(cudaStreamWaitEvent(e->copy_stream, e->ev_stage_free, 0));
             TRY_CUDA(cudaMemcpy2DAsync(e->d_fstage, row, fp, el * ldf, row, R,
-                                       cudaMemcpyHostToDevice, e->stream));
+                                       cudaMemcpyHostToDevice, e->copy_stream));
             if (beta != 0.0)
                 TRY_CUDA(cudaMemcpy2DAsync(e->d_ustage, row, up, el * ldu, row, R,
-                                           cudaMemcpyHostToDevice, e->stream));
+                                           cudaMemcpyHostToDevice, e->copy_stream));
+            TRY_CUDA(cudaEventRecord(e->ev_staged, e->copy_stream));
+            TRY_CUDA(cudaStreamWaitEvent(e->stream, e->ev_staged, 0));
             st = pass(e, R, e->d_fstage, 3L * n, e->d_ustage, 3L * n, alpha, beta);
             TRY(st);
             TRY_CUDA(cudaMemcpy2DAsync(up, el * ldu, e->d_ustage, row, row, R,
                                        cudaMemcpyDeviceToHost, e->stream));
+            TRY_CUDA(cudaEventRecord(e->ev_stage_free, e->stream));
         } else {
             st = pass(e, R, fp, ldf, up, ldu, alpha, beta);
             TRY(st);
