@@ -200,8 +200,8 @@ cudaError_t launch_interp_t(const InterpMaps &maps, const int *tile_off, const i
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    const bool use = CG == 4 ? maps.ok4 : maps.ok8;
-    const CUtensorMap &m = CG == 4 ? maps.cg4 : maps.cg8;
+    const bool use = maps.ok4;
+    const CUtensorMap &m = maps.cg4;
     kern<<<g.ntx * g.nty * g.ntz, kThreads, smem, s>>>(m, use ? 1 : 0, tile_off, rec_idx,
                                                       rec_start, rec_w, mesh, C, g, W,
                                                       accumulate, err);
@@ -212,9 +212,6 @@ template <typename T, int P>
 cudaError_t dispatch_cg(const InterpMaps &maps, const int *tile_off, const int *rec_idx,
                         const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
                         const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
-    if (interp_chunk(g, sizeof(T), C) == 8)
-        return launch_interp_t<T, P, 8>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W,
-                                        accumulate, err, s);
     return launch_interp_t<T, P, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W,
                                     accumulate, err, s);
 }
@@ -239,18 +236,12 @@ bool encode_box(CUtensorMap *m, const void *mesh, int K, int C, const MeshGeom &
 
 }  // namespace
 
-int interp_chunk(const MeshGeom &g, size_t elem, int C) {
-    const size_t plane = (size_t)(g.tz + g.p - 1) * (g.ty + g.p - 1) * kHX * elem;
-    return (C > 4 && 8 * plane + 128 <= 110 * 1024) ? 8 : 4;
-}
-
 size_t interp_smem_bytes(const MeshGeom &g, size_t elem) {
     return (size_t)4 * (g.tz + g.p - 1) * (g.ty + g.p - 1) * kHX * elem + 128;
 }
 
 bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem) {
     maps->ok4 = encode_box(&maps->cg4, mesh, g.K, C, g, elem, 4);
-    maps->ok8 = encode_box(&maps->cg8, mesh, g.K, C, g, elem, 8);
     return maps->ok4;
 }
 

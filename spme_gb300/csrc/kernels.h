@@ -51,16 +51,14 @@ bool spread_cols_ok(int K, int C, size_t elem);
 template <typename T>
 cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, const T *rec_w,
                                const T *Fs, int C, const MeshGeom &g, T *mesh, cudaStream_t s);
-// TMA descriptors of the real mesh [C][K][K][K] for the interpolation halo
-// boxes (4- and 8-component chunks).
+// TMA descriptor of the real mesh [C][K][K][K] for the interpolation halo
+// boxes (4 components per box: more blocks per SM than 8, measured faster).
 struct InterpMaps {
-    CUtensorMap cg4, cg8;
-    bool ok4 = false, ok8 = false;
+    CUtensorMap cg4;
+    bool ok4 = false;
 };
 bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem);
-// Components staged per chunk for C components (4 or 8).
-int interp_chunk(const MeshGeom &g, size_t elem, int C);
-// Shared memory the interpolation kernel needs with its narrowest (4-component) staging.
+// Shared memory the interpolation kernel needs (4-component boxes).
 size_t interp_smem_bytes(const MeshGeom &g, size_t elem);
 // err: device flag set to 1 if a TMA wait timed out.
 template <typename T>
