@@ -205,3 +205,34 @@ def test_column_gather_spread_matches_tile_spread(gpu_lib, case):
     assert relerr(out[1], out[0]) < 1e-13
     ref = oracle.recip(pos, L, xi, K, p, f, nthreads=4)
     assert relerr(out[1], ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("radius", [1.0, 1.5])
+def test_fp64_real_space_pairs_across_the_table_ranges(gpu_lib, radius):
+    """FP64 engines take F(r), G(r) from a Chebyshev table on [a/2, rc] and from
+    the closed form below a/2: pairs placed at separations on both sides of a/2,
+    inside and outside the overlap range 2a, and just inside rc, against the
+    oracle's closed form (FP64 1e-12)."""
+    a, L, rc, xi = radius, 60.0, 9.0, 0.4
+    seps = np.array([0.2, 0.49, 0.51, 0.8, 1.5, 1.99, 2.01, 2.5, 4.0, 7.3, 8.99]) * np.array(
+        [a] * 8 + [1.0] * 3)
+    rng = np.random.default_rng(17)
+    pos = []
+    for k, s in enumerate(seps):
+        c = np.array([5.0 + 11.0 * (k % 5), 5.0 + 11.0 * (k // 5), 30.0])
+        d = rng.standard_normal(3)
+        d *= s / np.linalg.norm(d)
+        pos += [c, c + d]
+    pos = np.mod(np.array(pos), L)
+    n = pos.shape[0]
+    f = rng.standard_normal((2, 3 * n))
+    eng = spme_gb300.Engine(n, L, xi, 32, 4, radius=a, rcut=rc, precision="fp64",
+                            max_nrhs=2, terms=spme_gb300.TERM_REAL | spme_gb300.TERM_SELF)
+    eng.set_positions(pos)
+    u = eng.apply(f)
+    eng.close()
+    ref = oracle.real_self(pos, L, xi, rc, f, radius=a, nthreads=2)
+    assert relerr(u, ref) < FP64_TOL
+    # the pair part alone (self term removed) at the same tolerance
+    self_c = oracle.self_coeff(xi, a)
+    assert relerr(u - self_c * f, ref - self_c * f) < 1e-11
