@@ -122,8 +122,14 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
     __shared__ G cx[kCap], cy[kCap], cz[kCap];
     __shared__ int cj[kCap];
     __shared__ int hits[kWarps][64];
-    __shared__ T pF[kWarps][32], pG[kWarps][32], pr[kWarps][3][32];
-    __shared__ int pj[kWarps][32];
+    // one record per buffered pair: unit vector and F in one 16/32-byte vector,
+    // then G and the start of the partner's force row
+    struct __align__(16) PairRec {
+        typename Geo4<T>::type rf;  // (rhat_x, rhat_y, rhat_z, F)
+        const T *frow;
+        T G;
+    };
+    __shared__ PairRec prec[kWarps][32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int cell = blockIdx.x;
@@ -221,21 +227,24 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
                     }
                     if (!done) real_FG<T>((T)rr, xi, a, Fv, Gv);
                     const G ir = G(1) / rr;
-                    pF[warp][lane] = Fv;
-                    pG[warp][lane] = Gv;
-                    pr[warp][0][lane] = (T)(d0 * ir);
-                    pr[warp][1][lane] = (T)(d1 * ir);
-                    pr[warp][2][lane] = (T)(d2 * ir);
-                    pj[warp][lane] = j;
+                    PairRec &pq = prec[warp][lane];
+                    pq.rf.x = (T)(d0 * ir);
+                    pq.rf.y = (T)(d1 * ir);
+                    pq.rf.z = (T)(d2 * ir);
+                    pq.rf.w = Fv;
+                    pq.G = Gv;
+                    pq.frow = F + (size_t)j * C;
                 }
                 __syncwarp();
                 s0 = s1 = s2 = T(0);
                 if (rok) {
                     for (int k = pp; k < m; k += PR) {
-                        const T *fj = F + (size_t)pj[warp][k] * C + 3 * r;
-                        const T f0 = fj[0], f1 = fj[1], f2 = fj[2];
-                        const T rx = pr[warp][0][k], ry = pr[warp][1][k], rz = pr[warp][2][k];
-                        const T Fk = pF[warp][k], Gd = pG[warp][k] * (rx * f0 + ry * f1 + rz * f2);
+                        const PairRec &pq = prec[warp][k];
+                        const auto rf = pq.rf;
+                        const T *fj = pq.frow + 3 * r;
+                        const T f0 = __ldg(fj), f1 = __ldg(fj + 1), f2 = __ldg(fj + 2);
+                        const T rx = rf.x, ry = rf.y, rz = rf.z;
+                        const T Fk = rf.w, Gd = pq.G * (rx * f0 + ry * f1 + rz * f2);
                         s0 += Fk * f0 + Gd * rx;
                         s1 += Fk * f1 + Gd * ry;
                         s2 += Fk * f2 + Gd * rz;
