@@ -692,8 +692,9 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         // column gather where it applies; measured on GB300 (K = 256, N = 1e6): in FP64
         // it wins at every C (8.0 vs 19.6 ms at C = 3), in FP32 from C = 9 on (the
         // tile kernel's per-component cost is lower at C = 3, 6)
+        // (the kernel stages force-row offsets s C as 32-bit integers)
         const bool use_cols = e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem) &&
-                              (e->elem == 8 || C >= 9);
+                              (e->elem == 8 || C >= 9) && (long long)n * C < (1LL << 31);
         if (use_cols) {
             spme::launch_gather_rows<T>(F, e->d_srec_idx, n, C, (T *)e->d_Fs, s);
             TRY_CUDA(spme::launch_spread_cols<T>(e->d_soff, e->d_srec_start,

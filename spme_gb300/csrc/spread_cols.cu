@@ -78,7 +78,7 @@ struct WarpScratch {
     // staged visit: w_x w_y w_z[j] for the pair's two columns (16-byte rows), then
     // (z offset, row of Fs)
     __align__(16) T wt[32][2][PW];
-    int2 dz_row[32];
+    int2 dz_row[32];  // (z offset, force-row offset s C)
     int begA[NQ], nA[NQ], begB[NQ];
     int pre[NQ + 1];
 };
@@ -117,6 +117,11 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
     for (int z = 0; z < TZ; z++)
 #pragma unroll
         for (int k = 0; k < CPL; k++) acc[z][k] = T(0);
+    // this lane's components: Fs + row offset + 16 k, valid where c < C
+    const T *fbase = Fs + cb + l16;
+    bool cval[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; k++) cval[k] = cb + l16 + 16 * k < C;
 
     if (xa < K) {
         // start-column table: z runs of start cells that reach [z0, z0 + ext),
@@ -181,7 +186,8 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 const int ox1 = ox + 1 == K ? 0 : ox + 1;
                 const T w0 = ox < P ? wy * __ldg(rw + ox) : T(0);
                 const T w1 = (ox1 < P && xa + 1 < K) ? wy * __ldg(rw + ox1) : T(0);
-                ws.dz_row[lane] = make_int2(sz - (partB ? z0 + K : z0), s);  // dz in [-(P-1), ext)
+                // dz in [-(P-1), ext); the visit's force row as an offset (s C < 2^31)
+                ws.dz_row[lane] = make_int2(sz - (partB ? z0 + K : z0), s * C);
                 T wz[P];
                 load_weights<T, P>(rw + 2 * P, wz);
                 // 16-byte stores (scalar stores at this lane stride conflict 16-way)
@@ -213,12 +219,9 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
             // accumulate the batch (force row of the next visit prefetched)
             T fn[CPL];
             {
-                const size_t frow = (size_t)ws.dz_row[0].y * C;
+                const T *row = fbase + ws.dz_row[0].y;
 #pragma unroll
-                for (int k = 0; k < CPL; k++) {
-                    const int c = cb + l16 + 16 * k;
-                    fn[k] = c < C ? __ldg(Fs + frow + c) : T(0);
-                }
+                for (int k = 0; k < CPL; k++) fn[k] = cval[k] ? __ldg(row + 16 * k) : T(0);
             }
             for (int j = 0; j < nb; j++) {
                 T f[CPL];
@@ -226,12 +229,9 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 for (int k = 0; k < CPL; k++) f[k] = fn[k];
                 const int2 dr = ws.dz_row[j];
                 if (j + 1 < nb) {
-                    const size_t frow = (size_t)ws.dz_row[j + 1].y * C;
+                    const T *row = fbase + ws.dz_row[j + 1].y;
 #pragma unroll
-                    for (int k = 0; k < CPL; k++) {
-                        const int c = cb + l16 + 16 * k;
-                        fn[k] = c < C ? __ldg(Fs + frow + c) : T(0);
-                    }
+                    for (int k = 0; k < CPL; k++) fn[k] = cval[k] ? __ldg(row + 16 * k) : T(0);
                 }
                 T wt[P];
                 load_weights<T, P>(&ws.wt[j][half][0], wt);
@@ -260,14 +260,20 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
 #pragma unroll
         for (int k = 0; k < CPL; k++) tsm[(size_t)(l16 + 16 * k) * ROW + z * XT + xl] = acc[z][k];
     __syncthreads();
-    // whole rows of XT columns per (component, plane)
-    const size_t KK = (size_t)K * K;
-    for (int row = threadIdx.x / XT; row < CC * TZ; row += (NW * 32) / XT) {
-        const int c = row / TZ, z = row - c * TZ;
-        const int x = threadIdx.x % XT;
-        if (cb + c < C && z < ext && x0 + x < K)
-            mesh[((size_t)(cb + c) * K + z0 + z) * KK + (size_t)y * K + x0 + x] =
-                tsm[(size_t)c * ROW + z * XT + x];
+    // whole rows of XT columns per (component, plane): each thread keeps one
+    // (plane, column) slot and walks the components with pointer increments
+    static_assert((NW * 32) % (XT * TZ) == 0 || (XT * TZ) % (NW * 32) == 0, "row split");
+    constexpr int SLOTS = XT * TZ;                    // (plane, column) slots of a component
+    constexpr int CSTEP = (NW * 32) >= SLOTS ? (NW * 32) / SLOTS : 1;  // components per sweep
+    const size_t K3 = (size_t)K * K * K;
+    const int nc = min(CC, C - cb);
+    for (int slot = threadIdx.x % SLOTS; slot < SLOTS; slot += NW * 32) {
+        const int z = slot / XT, x = slot - z * XT;
+        if (z >= ext || x0 + x >= K) continue;
+        T *out = mesh + (size_t)cb * K3 + ((size_t)(z0 + z) * K + y) * K + x0 + x;
+        const T *src = tsm + z * XT + x;
+        for (int c = threadIdx.x / SLOTS; c < nc; c += CSTEP)
+            out[(size_t)c * K3] = src[(size_t)c * ROW];
     }
 }
 
