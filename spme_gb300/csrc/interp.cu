@@ -159,15 +159,19 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
 #pragma unroll
             for (int k = 0; k < NG; k++) acc[k] = T(0);
             const T *base = box + (size_t)cl * PS + (lz * HYB + ly) * kHX + lx + xs;
+            // sum over y with w_x w_y first, then one w_z per plane
 #pragma unroll
             for (int z = 0; z < P; z++) {
                 const T *pz = base + z * HYB * kHX;
+                T t[NG];
 #pragma unroll
-                for (int y = 0; y < P; y++) {
-                    const T w = wz[z] * wxy[y];
+                for (int k = 0; k < NG; k++) t[k] = T(0);
 #pragma unroll
-                    for (int k = 0; k < NG; k++) acc[k] += w * pz[(size_t)k * 4 * PS + y * kHX];
-                }
+                for (int y = 0; y < P; y++)
+#pragma unroll
+                    for (int k = 0; k < NG; k++) t[k] += wxy[y] * pz[(size_t)k * 4 * PS + y * kHX];
+#pragma unroll
+                for (int k = 0; k < NG; k++) acc[k] += wz[z] * t[k];
             }
 #pragma unroll
             for (int k = 0; k < NG; k++)
