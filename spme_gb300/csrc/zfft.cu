@@ -303,21 +303,50 @@ constexpr ZCfg kCfg64[] = {{8, 384, 1, 6}, {4, 192, 2, 12}, {8, 192, 1, 12},
 // (chunk starts are multiples of W: 16-byte aligned in the global layout), all
 // 3R components.  Threads 0..CT-1 transform; the warp after them moves data: TMA loads into
 // the two buffers, TMA stores of finished buffers.
-// Pass sequence of the z transform: generic (from the plan) or, for KS = 256,
-// the two radix-16 passes with compile-time spans.
+// Compile-time pass sequences (codes and spans as in ZPlan, DIT order) for the
+// mesh sizes used most; any other K runs the plan's passes with runtime spans.
+template <int KS>
+struct ZFixed {
+    static constexpr int n = 0;
+    static constexpr int code[1] = {0}, span[1] = {0};
+};
+template <>
+struct ZFixed<128> {
+    static constexpr int n = 2;
+    static constexpr int code[2] = {44, 42}, span[2] = {1, 16};
+};
+template <>
+struct ZFixed<160> {
+    static constexpr int n = 3;
+    static constexpr int code[3] = {44, 21, 51}, span[3] = {1, 16, 32};
+};
+template <>
+struct ZFixed<256> {
+    static constexpr int n = 2;
+    static constexpr int code[2] = {44, 44}, span[2] = {1, 16};
+};
+
+// Passes I .. (DIF: down to 0, DIT: up to n - 1) of the fixed sequence of KS.
+template <typename T, int W, int CT, int KS, bool DIF, int I>
+__device__ __forceinline__ void zpasses_fixed(Cx<T> *cb, const Cx<T> *tw, int bi0) {
+    using Z = ZFixed<KS>;
+    constexpr int CODE = Z::code[I], SPAN = Z::span[I];
+    zpass<T, W, CT, CODE / 10, CODE % 10, DIF, KS, SPAN>(cb, KS, SPAN, tw, bi0);
+    if constexpr (DIF) {
+        compute_sync<CT>();
+        if constexpr (I > 0) zpasses_fixed<T, W, CT, KS, true, I - 1>(cb, tw, bi0);
+    } else if constexpr (I + 1 < Z::n) {
+        compute_sync<CT>();
+        zpasses_fixed<T, W, CT, KS, false, I + 1>(cb, tw, bi0);
+    }
+}
+
+// The z transform's passes: forward DIF (last pass first, each followed by a
+// barrier) or inverse DIT (first pass first, barriers between passes).
 template <typename T, int W, int CT, int KS, bool DIF>
 __device__ __forceinline__ void zpasses(Cx<T> *cb, const ZPlan &zp, const Cx<T> *tw, int bi0) {
-    if constexpr (KS == 256) {
-        if constexpr (DIF) {
-            zpass<T, W, CT, 4, 4, true, 256, 16>(cb, 256, 16, tw, bi0);
-            compute_sync<CT>();
-            zpass<T, W, CT, 4, 4, true, 256, 1>(cb, 256, 1, tw, bi0);
-            compute_sync<CT>();
-        } else {
-            zpass<T, W, CT, 4, 4, false, 256, 1>(cb, 256, 1, tw, bi0);
-            compute_sync<CT>();
-            zpass<T, W, CT, 4, 4, false, 256, 16>(cb, 256, 16, tw, bi0);
-        }
+    if constexpr (ZFixed<KS>::n > 0) {
+        zpasses_fixed<T, W, CT, KS, DIF, DIF ? ZFixed<KS>::n - 1 : 0>(cb, tw, bi0);
     } else {
         if constexpr (DIF) {
             for (int i = zp.npass - 1; i >= 0; i--) {
@@ -626,15 +655,29 @@ bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem) {
     return r == CUDA_SUCCESS;
 }
 
+template <int KS>
+bool plan_is(const ZPlan &zp) {
+    using Z = ZFixed<KS>;
+    if (zp.K != KS || zp.npass != Z::n) return false;
+    for (int i = 0; i < Z::n; i++)
+        if (zp.pcode[i] != Z::code[i] || zp.pspan[i] != Z::span[i]) return false;
+    return true;
+}
+
 template <typename T, int W, int CT, int MINB, int MAXP>
 cudaError_t launch_zcfg(const CUtensorMap &map, const T *tab2, const T *tw, const int *perm,
                         const ZPlan &zp, T twopi_L, int R, int zb, int *err, cudaStream_t s) {
-    // K = 256 with its usual plan (radix-16 passes of spans 1 and 16): the
-    // compile-time pass sequence
-    const bool k256 = zp.K == 256 && zp.npass == 2 && zp.pcode[0] == 44 && zp.pcode[1] == 44 &&
-                      zp.pspan[0] == 1 && zp.pspan[1] == 16;
-    auto kern = k256 ? k_zfft_influence<T, W, CT, MINB, MAXP, 256>
-                     : k_zfft_influence<T, W, CT, MINB, MAXP, 0>;
+    // a fixed pass sequence when the plan matches one (instantiated for each
+    // precision's first configuration, the one these K get)
+    constexpr ZCfg first = sizeof(T) == 4 ? kCfg32[0] : kCfg64[0];
+    constexpr bool fixed_ok = first.W == W && first.ct == CT && first.minb == MINB &&
+                              first.maxp == MAXP;
+    auto kern = k_zfft_influence<T, W, CT, MINB, MAXP, 0>;
+    if constexpr (fixed_ok) {
+        if (plan_is<256>(zp)) kern = k_zfft_influence<T, W, CT, MINB, MAXP, 256>;
+        if (plan_is<160>(zp)) kern = k_zfft_influence<T, W, CT, MINB, MAXP, 160>;
+        if (plan_is<128>(zp)) kern = k_zfft_influence<T, W, CT, MINB, MAXP, 128>;
+    }
     const int K = zp.K, Kh = K / 2 + 1;
     const size_t smem = zsmem_bytes<T>(K, W);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

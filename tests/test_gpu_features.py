@@ -191,12 +191,14 @@ def test_overlap_mode_matches_serial(gpu_lib):
     assert relerr((out[0] - 0.5) / 0.7, ref) < 1e-5
 
 
+@pytest.mark.parametrize("K", [128, 160, 256])
 @pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp64", 1e-13)])
-def test_fused_zfft_k256_matches_3d_fft(gpu_lib, prec, tol):
-    """K = 256 runs the compile-time pass sequence of the fused kernel; it must
-    agree with cuFFT's 3D path (validated against the oracle at other K)."""
-    n, L, K, p, R = 3000, 256.0, 256, 6, 3
-    pos, f = uniform_case(n, L, R, seed=256)
+def test_fused_zfft_fixed_sequence_matches_3d_fft(gpu_lib, K, prec, tol):
+    """K = 128, 160 and 256 run compile-time pass sequences of the fused kernel
+    (where the plan matches); they must agree with cuFFT's 3D path (validated
+    against the oracle at other K)."""
+    n, L, p, R = 3000, float(K), 6, 3
+    pos, f = uniform_case(n, L, R, seed=K)
     out = {}
     for mode in (0, 1):
         eng = spme_gb300.Engine(n, L, 0.4, K, p, precision=prec, max_nrhs=R,
