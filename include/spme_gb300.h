@@ -134,9 +134,11 @@ int spme_set_spread_mode(spme_t *spme, int mode);
 /* Transform strategy of the mesh pass.  1: cuFFT 2D (y, x) transforms of
  * every z-plane, then one fused kernel doing the z transform, the influence
  * and the inverse z transform in shared memory (one pass over the half
- * spectrum instead of three).  0: cuFFT 3D transforms and a separate
- * influence kernel.  Default: 1 in FP32 when K fits the fused kernel, else 0.
- * Mode 1 on an engine whose K does not fit returns SPME_ERR_UNSUPPORTED. */
+ * spectrum instead of three).  2: as 1 with this library's one-pass 2D
+ * transforms (FP32, K = 128, 160, 256; thread-block clusters exchange the
+ * row blocks of a plane).  0: cuFFT 3D transforms and a separate influence
+ * kernel.  Default: 1 in FP32 when K fits the fused kernel, else 0.  Modes 1
+ * and 2 on an engine they do not fit return SPME_ERR_UNSUPPORTED. */
 int spme_set_fft_mode(spme_t *spme, int mode);
 
 /* Capture each mesh pass (and each device-pointer position build) into a CUDA

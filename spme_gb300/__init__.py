@@ -337,7 +337,9 @@ class Engine:
         _check(load().spme_set_spread_mode(self.h, int(mode)), "spme_set_spread_mode")
 
     def set_fft_mode(self, mode: int):
-        """1: 2D cuFFT + fused z-FFT/influence kernel (default); 0: 3D cuFFT + influence."""
+        """2: one-pass 2D transforms + fused z-FFT/influence kernel (FP32, K = 128,
+        160, 256); 1: 2D cuFFT + fused kernel (the FP32 default where it fits);
+        0: 3D cuFFT + influence."""
         _check(load().spme_set_fft_mode(self.h, int(mode)), "spme_set_fft_mode")
 
     def set_tile(self, tx: int, ty: int, tz: int):

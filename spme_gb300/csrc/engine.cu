@@ -111,6 +111,7 @@ struct _spme_t {
     spme::ZPlan zp{};
     void *d_ztw = nullptr;
     int *d_zip = nullptr;
+    void *d_f2tab = nullptr;  // one-pass 2D transform tables (fft_mode 2)
     CUtensorMap zmap;  // over the half spectrum (fft_mode 1)
     size_t cap_tiles = 0;  // allocated tile-count capacity
     // CUDA graphs: passes and device-pointer position builds are captured once
@@ -456,6 +457,14 @@ int create_impl(const spme_params &prm, spme_t **out) {
             // measured on GB300 (K = 256): the fused path wins in FP32; in FP64
             // the 3D transforms + influence are as fast
             e->fft_mode = is_fp32(e) ? 1 : 0;
+            // tables of the one-pass 2D transforms (fft_mode 2, opt-in: measured
+            // slower than cuFFT's 2D transforms, 7.2 vs 2.5 ms at K = 256)
+            std::vector<unsigned char> f2;
+            if (e->fft_mode == 1 && spme::fft2d_ok((int)K, e->elem) &&
+                spme::make_fft2d_tables((int)K, &f2)) {
+                TRY(dalloc(&e->d_f2tab, f2.size()));
+                TRY_CUDA(cudaMemcpy(e->d_f2tab, f2.data(), f2.size(), cudaMemcpyHostToDevice));
+            }
         } else {
             e->fft_mode = 0;
         }
@@ -550,7 +559,7 @@ void destroy_impl(spme_t *e) {
                     e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_mesh,
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
-                    e->d_zip,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
+                    e->d_zip,    e->d_f2tab,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
                     e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2, e->d_pair, e->d_key2,
                     e->d_slot2,  e->d_key3,   e->d_slot3};
     for (void *b : bufs) dfree(b);
@@ -706,9 +715,16 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
                                             (const T *)e->d_rec_w, F, C, e->g, (T *)e->d_mesh, s));
         e->launches++;
         if (prof) cudaEventRecord(e->ev[2], s);
-        const bool fused = e->fft_mode == 1 && pp->has2d;
+        // fft_mode 2: this project's one-pass 2D transforms; 1: cuFFT's 2D
+        // transforms; both followed by the fused z transform + influence
+        const bool own2d = e->fft_mode == 2 && e->d_f2tab;
+        const bool fused = own2d || (e->fft_mode == 1 && pp->has2d);
         cufftHandle fwd = fused ? pp->fwd2 : pp->fwd, bwd = fused ? pp->bwd2 : pp->bwd;
-        if (sizeof(T) == 4)
+        if (own2d) {
+            TRY_CUDA(spme::launch_fft2d_r2c(K, (const float *)e->d_mesh, (float *)e->d_cmesh,
+                                            (long)C * K, e->d_f2tab, s));
+            e->launches++;
+        } else if (sizeof(T) == 4)
             TRY_FFT(cufftExecR2C(fwd, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh));
         else
             TRY_FFT(cufftExecD2Z(fwd, (cufftDoubleReal *)e->d_mesh,
@@ -725,7 +741,11 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
             e->launches += 2;
         }
         if (prof) cudaEventRecord(e->ev[4], s);
-        if (sizeof(T) == 4)
+        if (own2d) {
+            TRY_CUDA(spme::launch_fft2d_c2r(K, (const float *)e->d_cmesh, (float *)e->d_mesh,
+                                            (long)C * K, e->d_f2tab, s));
+            e->launches++;
+        } else if (sizeof(T) == 4)
             TRY_FFT(cufftExecC2R(bwd, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh));
         else
             TRY_FFT(cufftExecZ2D(bwd, (cufftDoubleComplex *)e->d_cmesh,
@@ -987,9 +1007,10 @@ int spme_set_spread_mode(spme_t *e, int mode) {
 }
 
 int spme_set_fft_mode(spme_t *e, int mode) {
-    if (!e || (mode != 0 && mode != 1)) return SPME_ERR_INVALID;
+    if (!e || mode < 0 || mode > 2) return SPME_ERR_INVALID;
     DeviceGuard dg(e->device);
-    if (mode == 1 && !e->d_ztw) return e->last_error = SPME_ERR_UNSUPPORTED;
+    if (mode >= 1 && !e->d_ztw) return e->last_error = SPME_ERR_UNSUPPORTED;
+    if (mode == 2 && !e->d_f2tab) return e->last_error = SPME_ERR_UNSUPPORTED;
     if (e->stream) cudaStreamSynchronize(e->stream);
     drop_graphs(e);
     if (mode == 1) {

@@ -90,6 +90,17 @@ struct ZPlan {
 bool make_zplan(int K, size_t elem, ZPlan *zp, std::vector<double> *tw, std::vector<int> *perm);
 // Columns per block for K (0 if K does not fit the fused kernel).
 int zfft_width(int K, size_t elem);
+// One-pass 2D (y, x) transforms of the mesh's z-planes (FP32; K = 128, 160,
+// 256): real planes [planes][K][K] <-> half spectra [planes][K][K/2+1], cuFFT's
+// layouts and unnormalised conventions.  tables: make_fft2d_tables' bytes on
+// the device.
+bool fft2d_ok(int K, size_t elem);
+size_t fft2d_table_bytes(int K);
+bool make_fft2d_tables(int K, std::vector<unsigned char> *out);
+cudaError_t launch_fft2d_r2c(int K, const float *mesh, float *G, long planes, const void *tables,
+                             cudaStream_t s);
+cudaError_t launch_fft2d_c2r(int K, const float *G, float *mesh, long planes, const void *tables,
+                             cudaStream_t s);
 // TMA descriptor over the half spectrum G[C][K][K][K/2+1] (complex of elem-byte
 // reals), z-planes viewed as flat rows.
 bool make_zfft_map(CUtensorMap *map, void *G, int K, int C, size_t elem);

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fft_small.cuh"
 #include "kernels.h"
 #include "tma.cuh"
 
@@ -42,78 +43,6 @@ namespace spme {
 namespace {
 
 constexpr int kZSmemCap = 224 * 1024;
-
-template <typename T>
-struct Cx {
-    T re, im;
-};
-
-template <typename T>
-__device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
-    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
-}
-template <typename T>
-__device__ __forceinline__ Cx<T> cadd(Cx<T> a, Cx<T> b) { return {a.re + b.re, a.im + b.im}; }
-template <typename T>
-__device__ __forceinline__ Cx<T> csub(Cx<T> a, Cx<T> b) { return {a.re - b.re, a.im - b.im}; }
-
-// cos and sin of 2 pi m / R for the radix-3 and radix-5 kernels
-template <int R>
-__device__ __forceinline__ double root_cos(int m);
-template <int R>
-__device__ __forceinline__ double root_sin(int m);
-template <>
-__device__ __forceinline__ double root_cos<3>(int m) { return m == 0 ? 1.0 : -0.5; }
-template <>
-__device__ __forceinline__ double root_sin<3>(int m) {
-    return m == 0 ? 0.0 : (m == 1 ? 0.86602540378443865 : -0.86602540378443865);
-}
-// cos(2 pi/5) = (sqrt 5 - 1)/4, cos(4 pi/5) = -(sqrt 5 + 1)/4
-template <>
-__device__ __forceinline__ double root_cos<5>(int m) {
-    return m == 0 ? 1.0 : ((m == 1 || m == 4) ? 0.30901699437494742 : -0.80901699437494742);
-}
-template <>
-__device__ __forceinline__ double root_sin<5>(int m) {
-    return m == 0 ? 0.0
-                  : (m == 1 ? 0.95105651629515357
-                            : (m == 2 ? 0.58778525229247313
-                                      : (m == 3 ? -0.58778525229247313 : -0.95105651629515357)));
-}
-
-// Radix-R DFT of v into o: o[p] = sum_q v[q] w^{pq}, w = e^{-2 pi i/R}
-// (forward) or its conjugate (INV).
-template <typename T, int R, bool INV>
-__device__ __forceinline__ void dft_small(const Cx<T> (&v)[R], Cx<T> (&o)[R]) {
-    if constexpr (R == 1) {
-        o[0] = v[0];
-    } else if constexpr (R == 2) {
-        o[0] = cadd(v[0], v[1]);
-        o[1] = csub(v[0], v[1]);
-    } else if constexpr (R == 4) {
-        const Cx<T> s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-        const Cx<T> s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
-        // -i d13 forward, +i d13 inverse
-        const Cx<T> jd = INV ? Cx<T>{-d13.im, d13.re} : Cx<T>{d13.im, -d13.re};
-        o[0] = cadd(s02, s13);
-        o[1] = cadd(d02, jd);
-        o[2] = csub(s02, s13);
-        o[3] = csub(d02, jd);
-    } else {
-#pragma unroll
-        for (int p = 0; p < R; p++) {
-            Cx<T> s = v[0];
-#pragma unroll
-            for (int q = 1; q < R; q++) {
-                const int m = (p * q) % R;
-                const T c = (T)root_cos<R>(m), sn = (T)(INV ? root_sin<R>(m) : -root_sin<R>(m));
-                s.re += v[q].re * c - v[q].im * sn;
-                s.im += v[q].re * sn + v[q].im * c;
-            }
-            o[p] = s;
-        }
-    }
-}
 
 // One pass = two consecutive radix stages (R1 with span L, then R2 with span
 // L R1; R2 = 1 for a single stage) done in registers, over every column of the

@@ -210,6 +210,39 @@ def test_fused_zfft_fixed_sequence_matches_3d_fft(gpu_lib, K, prec, tol):
     assert relerr(out[1], out[0]) < tol
 
 
+@pytest.mark.parametrize("K", [128, 160, 256])
+def test_fft2d_one_pass_matches_cufft(gpu_lib, K):
+    """fft_mode 2 (one-pass 2D transforms with a cluster exchange, FP32) against
+    cuFFT's 2D transforms (mode 1) and the 3D path (mode 0), and the full
+    operator against the oracle at K = 128."""
+    n, L, p, R = 3000, float(K), 6, 3
+    pos, f = uniform_case(n, L, R, seed=K + 1)
+    out = {}
+    for mode in (0, 1, 2):
+        eng = spme_gb300.Engine(n, L, 0.4, K, p, precision="fp32", max_nrhs=R,
+                                terms=spme_gb300.TERM_RECIP)
+        eng.set_fft_mode(mode)
+        eng.set_positions(pos)
+        out[mode] = eng.apply(f.astype(eng.dtype))
+        eng.close()
+    assert relerr(out[2], out[1]) < 2e-6
+    assert relerr(out[2], out[0]) < 2e-6
+    if K == 128:
+        ref = oracle.recip(pos, L, 0.4, K, p, f, nthreads=4)
+        assert relerr(out[2], ref) < 1e-5
+
+
+def test_fft2d_mode_unsupported(gpu_lib):
+    """Mode 2 exists only for FP32 and K = 128, 160, 256."""
+    pos, f = uniform_case(200, 40.0, 1, seed=3)
+    for K, prec in ((200, "fp32"), (256, "fp64")):
+        eng = spme_gb300.Engine(200, 40.0, 0.5, K, 4, precision=prec, max_nrhs=1,
+                                terms=spme_gb300.TERM_RECIP)
+        with pytest.raises(spme_gb300.SpmeError):
+            eng.set_fft_mode(2)
+        eng.close()
+
+
 @pytest.mark.parametrize("K,prec,tol", [(320, "fp32", 2e-6), (512, "fp32", 2e-6), (384, "fp64", 1e-13)])
 def test_fused_zfft_large_k_matches_3d_fft(gpu_lib, K, prec, tol):
     """K > 256: the fused kernel moves each z column as several TMA boxes
