@@ -3,7 +3,7 @@ normal forces, a few applies on the current CUDA device.  Small enough for
 multi-pass profiler captures (tens of passes per kernel).
 
   python -m spme_gb300.profile_case --n 100000 --box 480 --mesh 256 --order 6 \\
-      --nrhs 4 --terms recip [--tile 16,8,8] [--precision fp32] [--applies 2]
+      --nrhs 4 --terms recip [--tile 16,8,8] [--precision fp32] [--applies 2] [--fft-mode 2]
 """
 from __future__ import annotations
 
@@ -30,6 +30,7 @@ def main(argv=None) -> int:
     ap.add_argument("--tile", default=None, help="tx,ty,tz")
     ap.add_argument("--applies", type=int, default=2)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--fft-mode", type=int, default=None, help="0, 1 or 2 (see Engine.set_fft_mode)")
     a = ap.parse_args(argv)
 
     import torch
@@ -42,6 +43,8 @@ def main(argv=None) -> int:
     eng = Engine(a.n, a.box, a.xi, a.mesh, a.order, rcut=a.rcut, precision=a.precision,
                  max_nrhs=a.nrhs, terms=TERMS[a.terms])
     eng.set_graphs(False)
+    if a.fft_mode is not None:
+        eng.set_fft_mode(a.fft_mode)
     if a.tile:
         eng.set_tile(*(int(v) for v in a.tile.split(",")))
     eng.set_positions(pos)
