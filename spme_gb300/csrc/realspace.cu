@@ -82,6 +82,37 @@ __device__ __forceinline__ bool table_FG(const PairTable &tb, double r, double &
     return true;
 }
 
+// Accumulator across pair batches: FP64 engines add in FP64; FP32 engines add
+// in FP32 with Knuth's TwoSum error term carried alongside (the FP64 pipe is a
+// small fraction of the FP32 rate on this GPU, and a handful of double adds
+// per particle had become the kernel's limiter).
+template <typename T>
+struct PairSum {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T x) {
+        if constexpr (sizeof(T) == 8) {
+            s += x;
+        } else {
+            const T t = s + x, bp = t - s;
+            c += (s - (t - bp)) + (x - bp);
+            s = t;
+        }
+    }
+    __device__ __forceinline__ void add(const PairSum &o) {
+        add(o.s);
+        c += o.c;
+    }
+    __device__ __forceinline__ T value() const { return s + c; }
+};
+
+template <typename T>
+__device__ __forceinline__ PairSum<T> shfl_xor(const PairSum<T> &a, int o) {
+    PairSum<T> b;
+    b.s = __shfl_xor_sync(0xffffffffu, a.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, a.c, o);
+    return b;
+}
+
 template <typename G> struct Geo4;
 template <> struct Geo4<float> { using type = float4; };
 template <> struct Geo4<double> { using type = double4; };
@@ -202,7 +233,7 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
         for (int rb = 0; rb < R; rb += RL) {
             const int r = rb + rl;
             const bool rok = r < R;
-            double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+            PairSum<T> a0, a1, a2;
             int nh = 0;  // buffered hits (warp-uniform)
             // evaluate and apply `m` buffered hits; returns this lane's partial sums
             auto flush = [&](int m, T &s0, T &s1, T &s2) {
@@ -238,6 +269,7 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
                 __syncwarp();
                 s0 = s1 = s2 = T(0);
                 if (rok) {
+#pragma unroll 4
                     for (int k = pp; k < m; k += PR) {
                         const PairRec &pq = prec[warp][k];
                         const auto rf = pq.rf;
@@ -276,9 +308,9 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
                 if (nh >= 32) {
                     T s0, s1, s2;
                     flush(32, s0, s1, s2);
-                    a0 += (double)s0;
-                    a1 += (double)s1;
-                    a2 += (double)s2;
+                    a0.add(s0);
+                    a1.add(s1);
+                    a2.add(s2);
                     if (lane < nh - 32) hits[warp][lane] = hits[warp][32 + lane];
                     nh -= 32;
                     __syncwarp();
@@ -287,27 +319,27 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
             if (nh > 0) {
                 T s0, s1, s2;
                 flush(nh, s0, s1, s2);
-                a0 += (double)s0;
-                a1 += (double)s1;
-                a2 += (double)s2;
+                a0.add(s0);
+                a1.add(s1);
+                a2.add(s2);
             }
             // sum the PR pair slots of each right-hand side
             for (int o = RL; o < 32; o <<= 1) {
-                a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-                a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-                a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+                a0.add(shfl_xor(a0, o));
+                a1.add(shfl_xor(a1, o));
+                a2.add(shfl_xor(a2, o));
             }
             if (pp == 0 && rok) {
                 const T *fi = F + (size_t)ii * C + 3 * r;
                 if (with_self) {
-                    a0 += (double)self_c * (double)fi[0];
-                    a1 += (double)self_c * (double)fi[1];
-                    a2 += (double)self_c * (double)fi[2];
+                    a0.add(self_c * fi[0]);
+                    a1.add(self_c * fi[1]);
+                    a2.add(self_c * fi[2]);
                 }
                 T *o = W + (size_t)ii * C + 3 * r;
-                o[0] = (T)a0;
-                o[1] = (T)a1;
-                o[2] = (T)a2;
+                o[0] = a0.value();
+                o[1] = a1.value();
+                o[2] = a2.value();
             }
         }
     }
