@@ -61,22 +61,32 @@ __device__ __forceinline__ void bspline_weights(T w, T (&out)[P]) {
 // Multiplies by 1/L (FP64 division is slow); every kernel that needs a
 // particle's stencil start calls this same function, so sort keys and records
 // agree.
-__device__ __forceinline__ void mesh_coord(double x, double L, double invL, int K, int p,
-                                           int &start, double &frac) {
-    double xw = x - L * floor(x * invL);
+__device__ __forceinline__ double wrap_coord(double x, double L, double invL) {
+    return x - L * floor(x * invL);
+}
+// ... of a coordinate xw already wrapped into [0, L)
+__device__ __forceinline__ void mesh_coord_w(double xw, double invL, int K, int p, int &start,
+                                             double &frac) {
     double c = xw * invL * (double)K;
     double fl = floor(c);
     frac = c - fl;
     int s = (int)fl - p / 2 + 1;
     start = pmod(s, K);
 }
+__device__ __forceinline__ void mesh_coord(double x, double L, double invL, int K, int p,
+                                           int &start, double &frac) {
+    mesh_coord_w(wrap_coord(x, L, invL), invL, K, p, start, frac);
+}
 
 // Real-space cell (nc cells of edge L/nc per axis) of coordinate x, and x
 // wrapped into [0, L); shared by the cell keys and the cell-relative positions.
-__device__ __forceinline__ int cell_coord(double x, double L, double invL, int nc, double &xw) {
-    xw = x - L * floor(x * invL);
+__device__ __forceinline__ int cell_coord_w(double xw, double invL, int nc) {
     const int v = (int)(xw * invL * (double)nc);
     return v >= nc ? nc - 1 : (v < 0 ? 0 : v);
+}
+__device__ __forceinline__ int cell_coord(double x, double L, double invL, int nc, double &xw) {
+    xw = wrap_coord(x, L, invL);
+    return cell_coord_w(xw, invL, nc);
 }
 
 __device__ __forceinline__ uint32_t pack_start(int sx, int sy, int sz) {

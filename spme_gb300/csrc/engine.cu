@@ -82,6 +82,8 @@ struct _spme_t {
     // device buffers
     double *d_pos = nullptr;
     int *d_key2 = nullptr, *d_slot2 = nullptr, *d_key3 = nullptr, *d_slot3 = nullptr;
+    uint32_t *d_pstart = nullptr;  // per-particle stencil start (mesh engines)
+    void *d_pfrac = nullptr;       // per-particle fractional mesh coordinates
     int *d_key = nullptr, *d_slot = nullptr, *d_tcount = nullptr, *d_toff = nullptr,
         *d_tperm = nullptr, *d_scan_tmp = nullptr;
     int *d_rec_idx = nullptr;
@@ -388,6 +390,10 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY(dalloc(&e->d_key3, sizeof(int) * n));
     TRY(dalloc(&e->d_slot3, sizeof(int) * n));
     TRY(dalloc(&e->d_tperm, sizeof(int) * n));
+    if (prm.terms & SPME_TERM_RECIP) {
+        TRY(dalloc(&e->d_pstart, sizeof(uint32_t) * n));
+        TRY(dalloc(&e->d_pfrac, e->elem * 3 * n));
+    }
     e->cols = (prm.terms & SPME_TERM_RECIP) && spme::spread_cols_ok((int)K, (int)C, e->elem);
     if (e->cols) {
         const size_t K3 = K * K * K;
@@ -562,7 +568,7 @@ void destroy_impl(spme_t *e) {
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_f2tab,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
                     e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2, e->d_pair, e->d_key2,
-                    e->d_slot2,  e->d_key3,   e->d_slot3};
+                    e->d_slot2,  e->d_key3,   e->d_slot3, e->d_pstart, e->d_pfrac};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -601,29 +607,34 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
         // one pass over the positions for every key this engine sorts by
         spme::launch_all_keys(e->d_pos, n, e->g, e->nc, e->d_key, recip ? e->d_tcount : nullptr,
                               e->d_slot, e->d_key2, cols ? e->d_scount : nullptr, e->d_slot2,
-                              e->d_key3, real ? e->d_ccount : nullptr, e->d_slot3, s);
+                              e->d_key3, real ? e->d_ccount : nullptr, e->d_slot3,
+                              recip ? e->d_pstart : nullptr, e->d_pfrac, is_fp32(e), s);
         e->launches++;
     }
     if (recip) {
         spme::launch_scan(e->d_tcount, e->ntiles, e->d_toff, e->d_scan_tmp, s);
         spme::launch_scatter(e->d_key, e->d_slot, e->d_toff, n, e->d_tperm, s);
         if (is_fp32(e))
-            spme::launch_records<float>(e->d_pos, e->d_tperm, n, e->g, e->d_rec_idx,
-                                        e->d_rec_start, (float *)e->d_rec_w, s);
+            spme::launch_records<float>(e->d_pstart, (const float *)e->d_pfrac, e->d_tperm, n,
+                                        e->g.p, e->d_rec_idx, e->d_rec_start,
+                                        (float *)e->d_rec_w, s);
         else
-            spme::launch_records<double>(e->d_pos, e->d_tperm, n, e->g, e->d_rec_idx,
-                                         e->d_rec_start, (double *)e->d_rec_w, s);
+            spme::launch_records<double>(e->d_pstart, (const double *)e->d_pfrac, e->d_tperm, n,
+                                         e->g.p, e->d_rec_idx, e->d_rec_start,
+                                         (double *)e->d_rec_w, s);
         e->launches += 5;
     }
     if (cols) {
         spme::launch_scan(e->d_scount, K3, e->d_soff, e->d_scan_tmp, s);
         spme::launch_scatter(e->d_key2, e->d_slot2, e->d_soff, n, e->d_sperm, s);
         if (is_fp32(e))
-            spme::launch_records<float>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
-                                        e->d_srec_start, (float *)e->d_srec_w, s);
+            spme::launch_records<float>(e->d_pstart, (const float *)e->d_pfrac, e->d_sperm, n,
+                                        e->g.p, e->d_srec_idx, e->d_srec_start,
+                                        (float *)e->d_srec_w, s);
         else
-            spme::launch_records<double>(e->d_pos, e->d_sperm, n, e->g, e->d_srec_idx,
-                                         e->d_srec_start, (double *)e->d_srec_w, s);
+            spme::launch_records<double>(e->d_pstart, (const double *)e->d_pfrac, e->d_sperm, n,
+                                         e->g.p, e->d_srec_idx, e->d_srec_start,
+                                         (double *)e->d_srec_w, s);
         e->launches += 5;
     }
     if (real) {

@@ -16,10 +16,12 @@ namespace spme {
 // Sort keys with a slot within each key (atomic counts): the mesh tile of the
 // stencil start (key1), the stencil-start cell ((sy K + sx) K + sz, K^3 keys;
 // key2), the real-space cell (nc^3 cells of edge L/nc; key3), in one pass over
-// the positions.  A null count skips that key.
+// the positions.  A null count skips that key.  With a mesh key, pstart (n)
+// and pfrac (3n values of the engine's type: float when fp32) receive each
+// particle's packed stencil start and fractional mesh coordinates.
 void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
                      int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
-                     int *slot3, cudaStream_t s);
+                     int *slot3, uint32_t *pstart, void *pfrac, bool fp32, cudaStream_t s);
 // Real-space cell key (nc^3 cells of edge L/nc) and slot within its cell.
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
                       int *slot, cudaStream_t s);
@@ -30,10 +32,11 @@ void launch_scan(const int *count, int nkeys, int *off, int *tmp, cudaStream_t s
 // perm[off[key[i]] + slot[i]] = i
 void launch_scatter(const int *key, const int *slot, const int *off, int n, int *perm,
                     cudaStream_t s);
-// B-spline records in tile-sorted order: rec_idx[s] = perm[s], packed stencil
-// start, and p weights per axis (record width RecordWidth<T,P>).
+// B-spline records in sorted order (perm): rec_idx[s] = perm[s], the packed
+// stencil start, and p weights per axis (record width RecordWidth<T,P>), from
+// launch_all_keys' per-particle starts and fractional coordinates.
 template <typename T>
-void launch_records(const double *pos, const int *perm, int n, const MeshGeom &g,
+void launch_records(const uint32_t *pstart, const T *pfrac, const int *perm, int n, int p,
                     int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s);
 // Cell-sorted positions relative to their cell's lower corner (float4 or double4).
 void launch_cell_positions(const double *pos, const int *perm, int n, double L, int nc,

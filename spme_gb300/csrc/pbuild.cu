@@ -32,22 +32,32 @@ __global__ void k_cell_keys(const double *__restrict__ pos, int n, double L, int
 // tile of the stencil start (always), the stencil-start cell (key2, when
 // count2 is set) and the real-space cell (key3, when count3 is set), each with
 // its slot from an atomic count.
+// ... and, when the mesh keys are wanted, each particle's packed stencil start
+// and fractional mesh coordinates (read by the record builds, so the FP64
+// coordinate arithmetic runs once per particle).
+template <typename T>
 __global__ void k_all_keys(const double *__restrict__ pos, int n, MeshGeom g, int nc,
                            int *__restrict__ key1, int *__restrict__ count1,
                            int *__restrict__ slot1, int *__restrict__ key2,
                            int *__restrict__ count2, int *__restrict__ slot2,
                            int *__restrict__ key3, int *__restrict__ count3,
-                           int *__restrict__ slot3) {
+                           int *__restrict__ slot3, uint32_t *__restrict__ pstart,
+                           T *__restrict__ pfrac) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s[3] = {0, 0, 0}, cc[3] = {0, 0, 0};
+    double fr[3] = {0.0, 0.0, 0.0};
     const bool mesh = count1 || count2;  // the mesh geometry is set only then
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        const double x = pos[3 * i + d];
-        double fr, xw;
-        if (mesh) mesh_coord(x, g.L, g.invL, g.K, g.p, s[d], fr);
-        if (count3) cc[d] = cell_coord(x, g.L, g.invL, nc, xw);
+        const double xw = wrap_coord(pos[3 * i + d], g.L, g.invL);
+        if (mesh) mesh_coord_w(xw, g.invL, g.K, g.p, s[d], fr[d]);
+        if (count3) cc[d] = cell_coord_w(xw, g.invL, nc);
+    }
+    if (mesh && pstart) {
+        pstart[i] = pack_start(s[0], s[1], s[2]);
+#pragma unroll
+        for (int d = 0; d < 3; d++) pfrac[3 * i + d] = (T)fr[d];
     }
     if (count1) {
         const int k = ((s[2] / g.tz) * g.nty + s[1] / g.ty) * g.ntx + s[0] / g.tx;
@@ -164,23 +174,18 @@ __global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ s
 }
 
 template <typename T, int P>
-__global__ void k_records(const double *__restrict__ pos, const int *__restrict__ perm, int n,
-                          MeshGeom g, int *__restrict__ rec_idx,
+__global__ void k_records(const uint32_t *__restrict__ pstart, const T *__restrict__ pfrac,
+                          const int *__restrict__ perm, int n, int *__restrict__ rec_idx,
                           uint32_t *__restrict__ rec_start, T *__restrict__ rec_w) {
     constexpr int WS = RecordWidth<T, P>::value;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     int i = perm[s];
-    int st[3];
     T w[3][P];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        double fr;
-        mesh_coord(pos[3 * i + d], g.L, g.invL, g.K, P, st[d], fr);
-        bspline_weights<T, P>((T)fr, w[d]);
-    }
+    for (int d = 0; d < 3; d++) bspline_weights<T, P>(pfrac[3 * i + d], w[d]);
     rec_idx[s] = i;
-    rec_start[s] = pack_start(st[0], st[1], st[2]);
+    rec_start[s] = pstart[i];
     T *out = rec_w + (size_t)s * WS;
 #pragma unroll
     for (int d = 0; d < 3; d++)
@@ -219,10 +224,16 @@ inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
                      int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
-                     int *slot3, cudaStream_t s) {
-    if (n > 0)
-        k_all_keys<<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2, count2,
-                                                slot2, key3, count3, slot3);
+                     int *slot3, uint32_t *pstart, void *pfrac, bool fp32, cudaStream_t s) {
+    if (n <= 0) return;
+    if (fp32)
+        k_all_keys<float><<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2,
+                                                       count2, slot2, key3, count3, slot3, pstart,
+                                                       (float *)pfrac);
+    else
+        k_all_keys<double><<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2,
+                                                        count2, slot2, key3, count3, slot3, pstart,
+                                                        (double *)pfrac);
 }
 
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
@@ -246,13 +257,13 @@ void launch_scatter(const int *key, const int *slot, const int *off, int n, int 
 }
 
 template <typename T>
-void launch_records(const double *pos, const int *perm, int n, const MeshGeom &g,
+void launch_records(const uint32_t *pstart, const T *pfrac, const int *perm, int n, int p,
                     int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s) {
     if (n <= 0) return;
-    switch (g.p) {
-        case 4: k_records<T, 4><<<nblk(n, 128), 128, 0, s>>>(pos, perm, n, g, rec_idx, rec_start, rec_w); break;
-        case 6: k_records<T, 6><<<nblk(n, 128), 128, 0, s>>>(pos, perm, n, g, rec_idx, rec_start, rec_w); break;
-        case 8: k_records<T, 8><<<nblk(n, 128), 128, 0, s>>>(pos, perm, n, g, rec_idx, rec_start, rec_w); break;
+    switch (p) {
+        case 4: k_records<T, 4><<<nblk(n, 128), 128, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
+        case 6: k_records<T, 6><<<nblk(n, 128), 128, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
+        case 8: k_records<T, 8><<<nblk(n, 128), 128, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
         default: break;
     }
 }
@@ -268,9 +279,9 @@ void launch_cell_positions(const double *pos, const int *perm, int n, double L, 
                                                                       (double4 *)cpos);
 }
 
-template void launch_records<float>(const double *, const int *, int, const MeshGeom &, int *,
+template void launch_records<float>(const uint32_t *, const float *, const int *, int, int, int *,
                                     uint32_t *, float *, cudaStream_t);
-template void launch_records<double>(const double *, const int *, int, const MeshGeom &, int *,
-                                     uint32_t *, double *, cudaStream_t);
+template void launch_records<double>(const uint32_t *, const double *, const int *, int, int,
+                                     int *, uint32_t *, double *, cudaStream_t);
 
 }  // namespace spme
