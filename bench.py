@@ -46,14 +46,11 @@ WORKLOADS = {
 }
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) measured with
-# ncu at full size on the large workload, FP32, R = 16, tile 16x8x8 (a 1-pass metric
+# ncu at full size on the large workload, FP32, R = 16, tile 16x8x4 (a 1-pass metric
 # set); the command is in profiles/dram_large_fp32_r16.md.
 NCU_TRAFFIC = {
-    "large": {
-        "spread": 816367104 + 3164926464,      # k_spread_cols
-        "influence": 3329840128 + 3266490624,  # k_zfft_influence
-        "interp": 6412758016 + 195079680,      # k_interp
-    },
+    "large": {"spread": 817994752 + 3174224384, "influence": 3314256384 + 3188328448,
+              "interp": 9366775808 + 198807552},
 }
 
 
