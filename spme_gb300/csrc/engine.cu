@@ -61,6 +61,10 @@ struct _spme_t {
     // already queued on the main stream, e.g. a position build)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_staged = nullptr, ev_stage_free = nullptr;
+    // host-pointer applies: the result leaves in parts of right-hand sides, part k
+    // complete at ev_part[k]
+    static constexpr int kOutParts = 4;
+    cudaEvent_t ev_part[kOutParts] = {};
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int profiling = 0;  // 1: stage events; 2: events + real-space serialized
     cudaEvent_t ev[kStages + 1] = {};
@@ -375,6 +379,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY_CUDA(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_staged, cudaEventDisableTiming));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_stage_free, cudaEventDisableTiming));
+    for (cudaEvent_t &ev : e->ev_part) TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     e->stream = e->own_stream;
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
@@ -581,6 +586,8 @@ void destroy_impl(spme_t *e) {
     if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
     if (e->ev_staged) cudaEventDestroy(e->ev_staged);
     if (e->ev_stage_free) cudaEventDestroy(e->ev_stage_free);
+    for (cudaEvent_t ev : e->ev_part)
+        if (ev) cudaEventDestroy(ev);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
     delete e;
 }
@@ -670,7 +677,8 @@ int set_positions_impl(spme_t *e, const double *pos, int mem) {
 }
 
 template <typename T>
-int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alpha, double beta) {
+int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alpha, double beta,
+             int rpart) {
     const int n = e->prm.np, C = 3 * R, K = e->prm.dim;
     const int terms = e->prm.terms;
     cudaStream_t s = e->stream;
@@ -775,18 +783,31 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         // interpolation; the unpack adds the two
         T *Wm = rs ? (T *)e->d_W2 : W;
         if (!Wm) return SPME_ERR_STATE;
-        TRY_CUDA(spme::launch_interp<T>(pp->maps, e->d_toff, n, e->d_rec_idx, e->d_rec_start,
-                                        (const T *)e->d_rec_w, (const T *)e->d_mesh, C, e->g, Wm,
-                                        0, e->d_err, s));
-        e->launches++;
-        if (prof) cudaEventRecord(e->ev[6], s);
-        if (rs) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
-        spme::launch_unpack_tiled<T>(W, rs ? Wm : nullptr, n, R, alpha, beta, u, ldu, s);
+        // rpart > 0: interpolation and unpack in parts of rpart right-hand sides (a
+        // multiple of 4: 12 components, whole 4-component interpolation chunks),
+        // part k complete at ev_part[k], so a host copy of a part overlaps the
+        // next part's interpolation
+        const int rp = rpart > 0 ? rpart : R;
+        for (int r0 = 0, k = 0; r0 < R; r0 += rp, k++) {
+            const int r1 = std::min(R, r0 + rp);
+            TRY_CUDA(spme::launch_interp<T>(pp->maps, e->d_toff, n, e->d_rec_idx,
+                                            e->d_rec_start, (const T *)e->d_rec_w,
+                                            (const T *)e->d_mesh, C, 3 * r0, 3 * r1, e->g, Wm, 0,
+                                            e->d_err, s));
+            e->launches++;
+            if (prof && r1 == R) cudaEventRecord(e->ev[6], s);
+            if (rs && k == 0) TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
+            spme::launch_unpack_tiled<T>(W, rs ? Wm : nullptr, n, R, r0, r1, alpha, beta, u, ldu,
+                                         s);
+            if (r1 < R) e->launches++;
+            if (rpart > 0 && k < spme_t::kOutParts) TRY_CUDA(cudaEventRecord(e->ev_part[k], s));
+        }
     } else {
         TRY_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
         if (prof)
             for (int k = 2; k <= 6; k++) cudaEventRecord(e->ev[k], s);
-        spme::launch_unpack_tiled<T>(W, nullptr, n, R, alpha, beta, u, ldu, s);
+        spme::launch_unpack_tiled<T>(W, nullptr, n, R, 0, R, alpha, beta, u, ldu, s);
+        if (rpart > 0) TRY_CUDA(cudaEventRecord(e->ev_part[0], s));
     }
     e->launches++;
     if (prof) cudaEventRecord(e->ev[7], s);
@@ -808,10 +829,10 @@ int check_device_error(spme_t *e) {
 }
 
 int pass_body(spme_t *e, int R, const void *f, long ldf, void *u, long ldu, double alpha,
-              double beta) {
+              double beta, int rpart = 0) {
     if (is_fp32(e))
-        return run_pass<float>(e, R, (const float *)f, ldf, (float *)u, ldu, alpha, beta);
-    return run_pass<double>(e, R, (const double *)f, ldf, (double *)u, ldu, alpha, beta);
+        return run_pass<float>(e, R, (const float *)f, ldf, (float *)u, ldu, alpha, beta, rpart);
+    return run_pass<double>(e, R, (const double *)f, ldf, (double *)u, ldu, alpha, beta, rpart);
 }
 
 // One mesh pass of R right-hand sides, replayed from a CUDA graph when graphs
@@ -874,11 +895,34 @@ int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
                                            cudaMemcpyHostToDevice, e->copy_stream));
             TRY_CUDA(cudaEventRecord(e->ev_staged, e->copy_stream));
             TRY_CUDA(cudaStreamWaitEvent(e->stream, e->ev_staged, 0));
-            st = pass(e, R, e->d_fstage, 3L * n, e->d_ustage, 3L * n, alpha, beta);
-            TRY(st);
-            TRY_CUDA(cudaMemcpy2DAsync(up, el * ldu, e->d_ustage, row, row, R,
-                                       cudaMemcpyDeviceToHost, e->stream));
-            TRY_CUDA(cudaEventRecord(e->ev_stage_free, e->stream));
+            // With the mesh part and 8+ right-hand sides the result leaves in parts
+            // (multiples of 4 right-hand sides), each copied on the copy stream while
+            // the next part is interpolated: a direct pass (a captured graph would
+            // expose only its end); the launches it saves are negligible next to a
+            // pass of this size.
+            const int rpart = ((e->prm.terms & SPME_TERM_RECIP) && !e->profiling && R >= 8)
+                                  ? std::max(4, (R + spme_t::kOutParts - 1) / spme_t::kOutParts + 3) / 4 * 4
+                                  : 0;
+            if (rpart > 0) {
+                st = pass_body(e, R, e->d_fstage, 3L * n, e->d_ustage, 3L * n, alpha, beta, rpart);
+                TRY(st);
+                for (int q0 = 0, k = 0; q0 < R; q0 += rpart, k++) {
+                    const int q1 = std::min(R, q0 + rpart);
+                    TRY_CUDA(cudaStreamWaitEvent(e->copy_stream, e->ev_part[k], 0));
+                    TRY_CUDA(cudaMemcpy2DAsync(up + el * (size_t)q0 * ldu, el * ldu,
+                                               (const char *)e->d_ustage + row * q0, row, row,
+                                               q1 - q0, cudaMemcpyDeviceToHost, e->copy_stream));
+                }
+                // the next staging waits for these copies (same stream); the main
+                // stream's next pass waits for that staging
+                TRY_CUDA(cudaEventRecord(e->ev_stage_free, e->copy_stream));
+            } else {
+                st = pass(e, R, e->d_fstage, 3L * n, e->d_ustage, 3L * n, alpha, beta);
+                TRY(st);
+                TRY_CUDA(cudaMemcpy2DAsync(up, el * ldu, e->d_ustage, row, row, R,
+                                           cudaMemcpyDeviceToHost, e->stream));
+                TRY_CUDA(cudaEventRecord(e->ev_stage_free, e->stream));
+            }
         } else {
             st = pass(e, R, fp, ldf, up, ldu, alpha, beta);
             TRY(st);
@@ -886,6 +930,7 @@ int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
     }
     if (mem == SPME_MEM_HOST) {
         TRY_CUDA(cudaStreamSynchronize(e->stream));
+        TRY_CUDA(cudaStreamSynchronize(e->copy_stream));
         TRY(check_device_error(e));
     }
     return SPME_OK;

@@ -34,8 +34,8 @@ __global__ void __launch_bounds__(kThreads)
 k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
          const int *__restrict__ tile_off, const int *__restrict__ rec_idx,
          const uint32_t *__restrict__ rec_start, const T *__restrict__ rec_w,
-         const T *__restrict__ mesh, int C, MeshGeom g, T *__restrict__ W, int accumulate,
-         int *__restrict__ err) {
+         const T *__restrict__ mesh, int C, int cb, int ce, MeshGeom g, T *__restrict__ W,
+         int accumulate, int *__restrict__ err) {
     using V = typename Vec16<T>::type;
     constexpr int VW = Vec16<T>::n;
     constexpr int NV = kHX / VW;  // vectors per staged row
@@ -107,8 +107,8 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
     };
 
     int chunk = 0;
-    for (int c0 = 0; c0 < C; c0 += CG, chunk++) {
-        const int nc = min(CG, C - c0);
+    for (int c0 = cb; c0 < ce; c0 += CG, chunk++) {
+        const int nc = min(CG, ce - c0);
         if (tma) {
             if (threadIdx.x == 0) {
                 fence_proxy_async();  // order earlier generic reads of the box before the TMA write
@@ -198,7 +198,8 @@ size_t interp_smem(const MeshGeom &g) {
 template <typename T, int P, int CG>
 cudaError_t launch_interp_t(const InterpMaps &maps, const int *tile_off, const int *rec_idx,
                             const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
-                            const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
+                            int cb, int ce, const MeshGeom &g, T *W, int accumulate, int *err,
+                            cudaStream_t s) {
     const size_t smem = interp_smem<T, P, CG>(g);
     auto kern = k_interp<T, P, CG>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -207,7 +208,7 @@ cudaError_t launch_interp_t(const InterpMaps &maps, const int *tile_off, const i
     const bool use = maps.ok4;
     const CUtensorMap &m = maps.cg4;
     kern<<<g.ntx * g.nty * g.ntz, kThreads, smem, s>>>(m, use ? 1 : 0, tile_off, rec_idx,
-                                                      rec_start, rec_w, mesh, C, g, W,
+                                                      rec_start, rec_w, mesh, C, cb, ce, g, W,
                                                       accumulate, err);
     return cudaGetLastError();
 }
@@ -215,9 +216,10 @@ cudaError_t launch_interp_t(const InterpMaps &maps, const int *tile_off, const i
 template <typename T, int P>
 cudaError_t dispatch_cg(const InterpMaps &maps, const int *tile_off, const int *rec_idx,
                         const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
-                        const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
-    return launch_interp_t<T, P, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W,
-                                    accumulate, err, s);
+                        int cb, int ce, const MeshGeom &g, T *W, int accumulate, int *err,
+                        cudaStream_t s) {
+    return launch_interp_t<T, P, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, cb, ce, g,
+                                    W, accumulate, err, s);
 }
 
 bool encode_box(CUtensorMap *m, const void *mesh, int K, int C, const MeshGeom &g, size_t elem,
@@ -252,22 +254,26 @@ bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom 
 template <typename T>
 cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, const int *rec_idx,
                           const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
-                          const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
+                          int cb, int ce, const MeshGeom &g, T *W, int accumulate, int *err,
+                          cudaStream_t s) {
+    if (n <= 0 || cb >= ce) return cudaSuccess;
+    if (cb < 0 || ce > C) return cudaErrorInvalidValue;
     if (g.tx + 7 > kHX || g.tx + g.p - 1 > kHX) return cudaErrorInvalidValue;
     switch (g.p) {
-        case 4: return dispatch_cg<T, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, err, s);
-        case 6: return dispatch_cg<T, 6>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, err, s);
-        case 8: return dispatch_cg<T, 8>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, g, W, accumulate, err, s);
+        case 4: return dispatch_cg<T, 4>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, cb, ce, g, W, accumulate, err, s);
+        case 6: return dispatch_cg<T, 6>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, cb, ce, g, W, accumulate, err, s);
+        case 8: return dispatch_cg<T, 8>(maps, tile_off, rec_idx, rec_start, rec_w, mesh, C, cb, ce, g, W, accumulate, err, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
 template cudaError_t launch_interp<float>(const InterpMaps &, const int *, int, const int *,
                                           const uint32_t *, const float *, const float *, int,
-                                          const MeshGeom &, float *, int, int *, cudaStream_t);
+                                          int, int, const MeshGeom &, float *, int, int *,
+                                          cudaStream_t);
 template cudaError_t launch_interp<double>(const InterpMaps &, const int *, int, const int *,
                                            const uint32_t *, const double *, const double *, int,
-                                           const MeshGeom &, double *, int, int *, cudaStream_t);
+                                           int, int, const MeshGeom &, double *, int, int *,
+                                           cudaStream_t);
 
 }  // namespace spme

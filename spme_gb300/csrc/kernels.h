@@ -63,11 +63,13 @@ struct InterpMaps {
 bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem);
 // Shared memory the interpolation kernel needs (4-component boxes).
 size_t interp_smem_bytes(const MeshGeom &g, size_t elem);
-// err: device flag set to 1 if a TMA wait timed out.
+// Components [cb, ce) of the C-component mesh (cb a multiple of 4) into
+// W[n][C]; err: device flag set to 1 if a TMA wait timed out.
 template <typename T>
 cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, const int *rec_idx,
                           const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
-                          const MeshGeom &g, T *W, int accumulate, int *err, cudaStream_t s);
+                          int cb, int ce, const MeshGeom &g, T *W, int accumulate, int *err,
+                          cudaStream_t s);
 
 // ---- k-space influence (influence.cu) -------------------------------------
 // tab[(z*K + y)*Kh + kx] = (S(k)|b|^2 / V, S(k)|b|^2 / (V k^2)), zero at k = 0.
@@ -154,9 +156,10 @@ void launch_pack(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
 // both sides; W2 may be null (plain unpack).  Up to 48 KB of shared memory.
 template <typename T>
 void launch_pack_tiled(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
+// (launch_unpack_tiled: right-hand sides [r0, r1) of the R in W / W2.)
 template <typename T>
-void launch_unpack_tiled(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
-                         long ld, cudaStream_t s);
+void launch_unpack_tiled(const T *W, const T *W2, int n, int R, int r0, int r1, double alpha,
+                         double beta, T *u, long ld, cudaStream_t s);
 template <typename T>
 void launch_unpack(const T *W, int n, int R, double alpha, double beta, T *u, long ld,
                    cudaStream_t s);

@@ -85,24 +85,24 @@ k_pack_tiled(const T *__restrict__ f, long ld, int n, int R, int pb, T *__restri
 // u = alpha (W [+ W2]) + beta u, tiled as k_pack_tiled.
 template <typename T, bool SUM>
 __global__ void __launch_bounds__(256)
-k_unpack_tiled(const T *__restrict__ W, const T *__restrict__ W2, int n, int R, int pb, T alpha,
-               T beta, T *__restrict__ u, long ld) {
+k_unpack_tiled(const T *__restrict__ W, const T *__restrict__ W2, int n, int R, int r0, int r1,
+               int pb, T alpha, T beta, T *__restrict__ u, long ld) {
     extern __shared__ __align__(16) unsigned char pk_raw[];
-    T *tile = reinterpret_cast<T *>(pk_raw);  // [pb][C + 1]
-    const int C = 3 * R, CS = C + 1;
+    T *tile = reinterpret_cast<T *>(pk_raw);  // [pb][CP + 1]
+    const int C = 3 * R, CP = 3 * (r1 - r0), CS = CP + 1;  // row stride, columns taken
     for (int i0 = blockIdx.x * pb; i0 < n; i0 += gridDim.x * pb) {
         const int np = min(pb, n - i0);
-        for (int t = threadIdx.x; t < np * C; t += blockDim.x) {
-            const int p = t / C, c = t - p * C;
-            const size_t k = (size_t)(i0 + p) * C + c;
+        for (int t = threadIdx.x; t < np * CP; t += blockDim.x) {
+            const int p = t / CP, c = t - p * CP;
+            const size_t k = (size_t)(i0 + p) * C + 3 * r0 + c;
             tile[p * CS + c] = SUM ? W[k] + W2[k] : W[k];
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < R * 3 * np; t += blockDim.x) {
+        for (int t = threadIdx.x; t < (r1 - r0) * 3 * np; t += blockDim.x) {
             const int r = t / (3 * np), q = t - r * 3 * np;
             const int p = q / 3, d = q - p * 3;
             const T w = tile[p * CS + 3 * r + d];
-            T *o = u + (size_t)r * ld + (size_t)3 * i0 + q;
+            T *o = u + (size_t)(r0 + r) * ld + (size_t)3 * i0 + q;
             *o = beta == T(0) ? alpha * w : beta * *o + alpha * w;
         }
         __syncthreads();
@@ -169,17 +169,17 @@ void launch_pack_tiled(const T *f, long ld, int n, int R, T *F, cudaStream_t s) 
 }
 
 template <typename T>
-void launch_unpack_tiled(const T *W, const T *W2, int n, int R, double alpha, double beta, T *u,
-                         long ld, cudaStream_t s) {
-    if (n <= 0 || R <= 0) return;
-    const int pb = tile_particles(R, sizeof(T));
-    const size_t smem = (size_t)pb * (3 * R + 1) * sizeof(T);
+void launch_unpack_tiled(const T *W, const T *W2, int n, int R, int r0, int r1, double alpha,
+                         double beta, T *u, long ld, cudaStream_t s) {
+    if (n <= 0 || R <= 0 || r0 < 0 || r1 > R || r0 >= r1) return;
+    const int pb = tile_particles(r1 - r0, sizeof(T));
+    const size_t smem = (size_t)pb * (3 * (r1 - r0) + 1) * sizeof(T);
     if (W2)
-        k_unpack_tiled<T, true><<<tiled_blocks(n, pb), 256, smem, s>>>(W, W2, n, R, pb, (T)alpha,
-                                                                        (T)beta, u, ld);
+        k_unpack_tiled<T, true><<<tiled_blocks(n, pb), 256, smem, s>>>(W, W2, n, R, r0, r1, pb,
+                                                                        (T)alpha, (T)beta, u, ld);
     else
-        k_unpack_tiled<T, false><<<tiled_blocks(n, pb), 256, smem, s>>>(W, W, n, R, pb, (T)alpha,
-                                                                         (T)beta, u, ld);
+        k_unpack_tiled<T, false><<<tiled_blocks(n, pb), 256, smem, s>>>(W, W, n, R, r0, r1, pb,
+                                                                         (T)alpha, (T)beta, u, ld);
 }
 
 template <typename T>
@@ -190,10 +190,10 @@ void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s) 
 
 template void launch_pack_tiled<float>(const float *, long, int, int, float *, cudaStream_t);
 template void launch_pack_tiled<double>(const double *, long, int, int, double *, cudaStream_t);
-template void launch_unpack_tiled<float>(const float *, const float *, int, int, double, double,
-                                         float *, long, cudaStream_t);
-template void launch_unpack_tiled<double>(const double *, const double *, int, int, double,
-                                          double, double *, long, cudaStream_t);
+template void launch_unpack_tiled<float>(const float *, const float *, int, int, int, int, double,
+                                         double, float *, long, cudaStream_t);
+template void launch_unpack_tiled<double>(const double *, const double *, int, int, int, int,
+                                          double, double, double *, long, cudaStream_t);
 template void launch_self<float>(const float *, int, int, double, float *, cudaStream_t);
 template void launch_self<double>(const double *, int, int, double, double *, cudaStream_t);
 template void launch_gather_rows<float>(const float *, const int *, int, int, float *,

@@ -262,3 +262,25 @@ def test_fused_zfft_large_k_matches_3d_fft(gpu_lib, K, prec, tol):
         out[mode] = eng.apply(f.astype(eng.dtype))
         eng.close()
     assert relerr(out[1], out[0]) < tol
+
+
+@pytest.mark.parametrize("R", [8, 12, 16])
+def test_host_apply_in_parts_matches_device(gpu_lib, R):
+    """Host-buffer applies with 8+ right-hand sides copy the result out in parts of
+    4 right-hand sides while the next part is interpolated; the values are those of
+    the device-pointer apply (same kernels, bit for bit), with alpha and beta."""
+    torch = pytest.importorskip("torch")
+    n, L, K, p = 2000, 30.0, 32, 6
+    pos, f = uniform_case(n, L, R, seed=R)
+    eng = spme_gb300.Engine(n, L, 0.4, K, p, rcut=6.0, precision="fp32", max_nrhs=R)
+    eng.set_positions(pos)
+    f32 = f.astype(np.float32)
+    u0 = np.random.default_rng(R).standard_normal((R, 3 * n)).astype(np.float32)
+    uh = eng.apply(f32, u0.copy(), alpha=0.7, beta=0.3)
+    fd = torch.tensor(f32, device="cuda")
+    ud = torch.tensor(u0, device="cuda")
+    eng.apply(fd, ud, alpha=0.7, beta=0.3)
+    assert np.array_equal(uh, ud.cpu().numpy())
+    ref = oracle.full(pos, L, 0.4, 6.0, K, p, f, nthreads=4)
+    assert relerr((uh - 0.3 * u0) / 0.7, ref) < 1e-5
+    eng.close()
