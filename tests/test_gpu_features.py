@@ -281,6 +281,11 @@ def test_host_apply_in_parts_matches_device(gpu_lib, R):
     ud = torch.tensor(u0, device="cuda")
     eng.apply(fd, ud, alpha=0.7, beta=0.3)
     assert np.array_equal(uh, ud.cpu().numpy())
+    # pinned host rows: the forces are packed in place from host memory
+    fp = torch.tensor(f32).pin_memory().numpy()
+    up = torch.tensor(u0).pin_memory().numpy()
+    eng.apply(fp, up, alpha=0.7, beta=0.3)
+    assert np.array_equal(up, uh)
     ref = oracle.full(pos, L, 0.4, 6.0, K, p, f, nthreads=4)
     assert relerr((uh - 0.3 * u0) / 0.7, ref) < 1e-5
     eng.close()
