@@ -317,23 +317,52 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
     TRY_FFT(cufftSetStream(pp.bwd, e->stream));
     if (e->fft_mode == 1) {
         // 2D (y, x) transforms of the C*K z-planes: same memory layout as the
-        // 3D transform's first two stages
+        // 3D transform's first two stages.  Two candidates per direction, cuFFT's
+        // default kernels and its patient-JIT search, which is faster at some sizes
+        // and slower at others on GB300 (K = 256: 2.44 vs 2.56 ms per direction;
+        // K = 160: 0.84 vs 0.80 ms); both are timed once and the faster is kept.
         const int Khp = K / 2 + 1;
         int n2[2] = {K, K}, re2[2] = {K, K}, ce2[2] = {K, Khp};
-        size_t w3 = 0, w4 = 0;
-        TRY_FFT(cufftCreate(&pp.fwd2));
-        TRY_FFT(cufftCreate(&pp.bwd2));
-        TRY_FFT(cufftSetAutoAllocation(pp.fwd2, 0));
-        TRY_FFT(cufftSetAutoAllocation(pp.bwd2, 0));
         const int P2 = K * K, C2 = K * Khp;
-        TRY_FFT(cufftMakePlanMany(pp.fwd2, 2, n2, re2, 1, P2, ce2, 1, C2, tf, C * K, &w3));
-        TRY_FFT(cufftMakePlanMany(pp.bwd2, 2, n2, ce2, 1, C2, re2, 1, P2, tb, C * K, &w4));
-        const size_t ws2d = std::max(w3, w4);
+        cufftHandle cand[2][2] = {{0, 0}, {0, 0}};  // [inverse][patient]
+        auto drop = [&]() {
+            for (auto &row : cand)
+                for (cufftHandle &h : row)
+                    if (h) cufftDestroy(h);
+        };
+        size_t ws2d = 0;
+        for (int d = 0; d < 2; d++)
+            for (int pt = 0; pt < 2; pt++) {
+                cufftHandle h = 0;
+                if (cufftCreate(&h) != CUFFT_SUCCESS) continue;
+                bool ok = cufftSetAutoAllocation(h, 0) == CUFFT_SUCCESS;
+                if (ok && pt)
+                    ok = cufftSetPlanPropertyInt64(h, NVFFT_PLAN_PROPERTY_INT64_PATIENT_JIT, 1) ==
+                         CUFFT_SUCCESS;
+                size_t w = 0;
+                if (ok)
+                    ok = (d == 0 ? cufftMakePlanMany(h, 2, n2, re2, 1, P2, ce2, 1, C2, tf, C * K, &w)
+                                 : cufftMakePlanMany(h, 2, n2, ce2, 1, C2, re2, 1, P2, tb, C * K,
+                                                     &w)) == CUFFT_SUCCESS;
+                if (!ok) {
+                    cufftDestroy(h);
+                    continue;
+                }
+                cand[d][pt] = h;
+                ws2d = std::max(ws2d, w);
+            }
+        if (!cand[0][0] || !cand[1][0]) {
+            drop();
+            return SPME_ERR_CUDA;
+        }
         if (ws2d > e->work_bytes) {
             dfree(e->d_work);
             e->d_work = nullptr;
             e->work_bytes = 0;
-            TRY(dalloc(&e->d_work, ws2d));
+            if (dalloc(&e->d_work, ws2d) != SPME_OK) {
+                drop();
+                return SPME_ERR_NOMEM;
+            }
             e->work_bytes = ws2d;
             for (PlanPair &q : e->plans) {
                 TRY_FFT(cufftSetWorkArea(q.fwd, e->d_work));
@@ -346,10 +375,50 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
             TRY_FFT(cufftSetWorkArea(pp.fwd, e->d_work));
             TRY_FFT(cufftSetWorkArea(pp.bwd, e->d_work));
         }
-        TRY_FFT(cufftSetWorkArea(pp.fwd2, e->d_work));
-        TRY_FFT(cufftSetWorkArea(pp.bwd2, e->d_work));
-        TRY_FFT(cufftSetStream(pp.fwd2, e->stream));
-        TRY_FFT(cufftSetStream(pp.bwd2, e->stream));
+        for (auto &row : cand)
+            for (cufftHandle h : row)
+                if (h) {
+                    cufftSetWorkArea(h, e->d_work);
+                    cufftSetStream(h, e->stream);
+                }
+        // time each direction's candidates (one warm and one timed run on the
+        // engine's mesh buffers, whose contents the next pass overwrites); not
+        // while the stream is being captured
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(e->stream, &cs);
+        auto exec = [&](cufftHandle h, int d) {
+            if (is_fp32(e))
+                return d == 0 ? cufftExecR2C(h, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh)
+                              : cufftExecC2R(h, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh);
+            return d == 0 ? cufftExecD2Z(h, (cufftDoubleReal *)e->d_mesh,
+                                         (cufftDoubleComplex *)e->d_cmesh)
+                          : cufftExecZ2D(h, (cufftDoubleComplex *)e->d_cmesh,
+                                         (cufftDoubleReal *)e->d_mesh);
+        };
+        auto time_ms = [&](cufftHandle h, int d) -> float {
+            if (exec(h, d) != CUFFT_SUCCESS) return -1.f;
+            cudaEventRecord(e->ev[0], e->stream);
+            if (exec(h, d) != CUFFT_SUCCESS) return -1.f;
+            cudaEventRecord(e->ev[1], e->stream);
+            float ms = -1.f;
+            if (cudaEventSynchronize(e->ev[1]) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]) != cudaSuccess)
+                return -1.f;
+            return ms;
+        };
+        cufftHandle pick[2];
+        for (int d = 0; d < 2; d++) {
+            int k = 0;
+            if (cand[d][1] && cs == cudaStreamCaptureStatusNone) {
+                const float t0 = time_ms(cand[d][0], d), t1 = time_ms(cand[d][1], d);
+                if (t1 > 0.f && t0 > 0.f && t1 < t0) k = 1;
+            }
+            pick[d] = cand[d][k];
+            if (cand[d][1 - k]) cufftDestroy(cand[d][1 - k]);
+        }
+        TRY_CUDA(cudaGetLastError());
+        pp.fwd2 = pick[0];
+        pp.bwd2 = pick[1];
         pp.has2d = true;
     }
     e->plans.push_back(pp);
