@@ -102,6 +102,7 @@ struct _spme_t {
     void *d_Fs = nullptr;  // force rows in start-cell order
     int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
     void *d_cpos = nullptr;  // float4 (FP32 engine) or double4 (FP64 engine)
+    void *d_prel = nullptr;  // the same in particle order (from the keys pass)
     void *d_pair = nullptr;  // Chebyshev table of the pair functions (FP64 engines)
     spme::PairTable pair;
     void *d_mesh = nullptr, *d_cmesh = nullptr, *d_tab = nullptr;
@@ -491,6 +492,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_coff, sizeof(int) * (ncell + 1)));
         TRY(dalloc(&e->d_cperm, sizeof(int) * n));
         TRY(dalloc(&e->d_cpos, sizeof(double4) * n));
+        TRY(dalloc(&e->d_prel, sizeof(double4) * n));
         // FP64: the pair functions from a Chebyshev table instead of erfc / exp
         std::vector<double> coef;
         if (!is_fp32(e) && spme::build_pair_table(prm.xi, prm.radius, prm.rcut, &coef, &e->pair)) {
@@ -637,7 +639,7 @@ void destroy_impl(spme_t *e) {
     }
     void *bufs[] = {e->d_pos,    e->d_key,     e->d_slot,  e->d_tcount,   e->d_toff,
                     e->d_tperm,  e->d_scan_tmp, e->d_rec_idx, e->d_rec_start, e->d_rec_w,
-                    e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_mesh,
+                    e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_prel, e->d_mesh,
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_f2tab,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
@@ -684,7 +686,8 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
         spme::launch_all_keys(e->d_pos, n, e->g, e->nc, e->d_key, recip ? e->d_tcount : nullptr,
                               e->d_slot, e->d_key2, cols ? e->d_scount : nullptr, e->d_slot2,
                               e->d_key3, real ? e->d_ccount : nullptr, e->d_slot3,
-                              recip ? e->d_pstart : nullptr, e->d_pfrac, is_fp32(e), s);
+                              recip ? e->d_pstart : nullptr, e->d_pfrac,
+                              real ? e->d_prel : nullptr, is_fp32(e), s);
         e->launches++;
     }
     if (recip) {
@@ -716,8 +719,7 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
     if (real) {
         spme::launch_scan(e->d_ccount, ncell, e->d_coff, e->d_scan_tmp, s);
         spme::launch_scatter(e->d_key3, e->d_slot3, e->d_coff, n, e->d_cperm, s);
-        spme::launch_cell_positions(e->d_pos, e->d_cperm, n, e->prm.box_size, e->nc, is_fp32(e),
-                                    e->d_cpos, s);
+        spme::launch_cell_gather(e->d_prel, e->d_cperm, n, is_fp32(e), e->d_cpos, s);
         e->launches += 5;
     }
     TRY_CUDA(cudaGetLastError());

@@ -18,10 +18,15 @@ namespace spme {
 // key2), the real-space cell (nc^3 cells of edge L/nc; key3), in one pass over
 // the positions.  A null count skips that key.  With a mesh key, pstart (n)
 // and pfrac (3n values of the engine's type: float when fp32) receive each
-// particle's packed stencil start and fractional mesh coordinates.
+// particle's packed stencil start and fractional mesh coordinates; with the
+// cell key, prel (n float4 / double4) its position relative to its cell.
 void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
                      int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
-                     int *slot3, uint32_t *pstart, void *pfrac, bool fp32, cudaStream_t s);
+                     int *slot3, uint32_t *pstart, void *pfrac, void *prel, bool fp32,
+                     cudaStream_t s);
+// cpos[s] = prel[perm[s]] (float4 or double4): cell-relative positions in cell order.
+void launch_cell_gather(const void *prel, const int *perm, int n, bool fp32, void *cpos,
+                        cudaStream_t s);
 // Real-space cell key (nc^3 cells of edge L/nc) and slot within its cell.
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
                       int *slot, cudaStream_t s);

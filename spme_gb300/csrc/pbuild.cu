@@ -33,8 +33,13 @@ __global__ void k_cell_keys(const double *__restrict__ pos, int n, double L, int
 // count2 is set) and the real-space cell (key3, when count3 is set), each with
 // its slot from an atomic count.
 // ... and, when the mesh keys are wanted, each particle's packed stencil start
-// and fractional mesh coordinates (read by the record builds, so the FP64
-// coordinate arithmetic runs once per particle).
+// and fractional mesh coordinates (read by the record builds), and with the cell
+// key its position relative to its cell's lower corner (gathered into cell
+// order later), so the FP64 coordinate arithmetic runs once per particle.
+template <typename T> struct Vec4T;
+template <> struct Vec4T<float> { using type = float4; };
+template <> struct Vec4T<double> { using type = double4; };
+
 template <typename T>
 __global__ void k_all_keys(const double *__restrict__ pos, int n, MeshGeom g, int nc,
                            int *__restrict__ key1, int *__restrict__ count1,
@@ -42,17 +47,29 @@ __global__ void k_all_keys(const double *__restrict__ pos, int n, MeshGeom g, in
                            int *__restrict__ count2, int *__restrict__ slot2,
                            int *__restrict__ key3, int *__restrict__ count3,
                            int *__restrict__ slot3, uint32_t *__restrict__ pstart,
-                           T *__restrict__ pfrac) {
+                           T *__restrict__ pfrac, typename Vec4T<T>::type *__restrict__ prel) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s[3] = {0, 0, 0}, cc[3] = {0, 0, 0};
-    double fr[3] = {0.0, 0.0, 0.0};
+    double fr[3] = {0.0, 0.0, 0.0}, rel[3] = {0.0, 0.0, 0.0};
     const bool mesh = count1 || count2;  // the mesh geometry is set only then
+    const double h = g.L / nc;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const double xw = wrap_coord(pos[3 * i + d], g.L, g.invL);
         if (mesh) mesh_coord_w(xw, g.invL, g.K, g.p, s[d], fr[d]);
-        if (count3) cc[d] = cell_coord_w(xw, g.invL, nc);
+        if (count3) {
+            cc[d] = cell_coord_w(xw, g.invL, nc);
+            rel[d] = xw - cc[d] * h;
+        }
+    }
+    if (count3 && prel) {
+        typename Vec4T<T>::type v;
+        v.x = (T)rel[0];
+        v.y = (T)rel[1];
+        v.z = (T)rel[2];
+        v.w = T(0);
+        prel[i] = v;
     }
     if (mesh && pstart) {
         pstart[i] = pack_start(s[0], s[1], s[2]);
@@ -195,6 +212,14 @@ __global__ void k_records(const uint32_t *__restrict__ pstart, const T *__restri
     for (int j = 3 * P; j < WS; j++) out[j] = T(0);
 }
 
+// Cell-relative positions in cell order, gathered from the keys pass's output.
+template <typename G4>
+__global__ void k_cell_gather(const G4 *__restrict__ prel, const int *__restrict__ perm, int n,
+                              G4 *__restrict__ cpos) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) cpos[s] = prel[perm[s]];
+}
+
 // Positions relative to the lower corner of their real-space cell.
 template <typename G4, typename G>
 __global__ void k_cell_positions(const double *__restrict__ pos, const int *__restrict__ perm,
@@ -224,16 +249,28 @@ inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
                      int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
-                     int *slot3, uint32_t *pstart, void *pfrac, bool fp32, cudaStream_t s) {
+                     int *slot3, uint32_t *pstart, void *pfrac, void *prel, bool fp32,
+                     cudaStream_t s) {
     if (n <= 0) return;
     if (fp32)
         k_all_keys<float><<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2,
                                                        count2, slot2, key3, count3, slot3, pstart,
-                                                       (float *)pfrac);
+                                                       (float *)pfrac, (float4 *)prel);
     else
         k_all_keys<double><<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2,
                                                         count2, slot2, key3, count3, slot3, pstart,
-                                                        (double *)pfrac);
+                                                        (double *)pfrac, (double4 *)prel);
+}
+
+void launch_cell_gather(const void *prel, const int *perm, int n, bool fp32, void *cpos,
+                        cudaStream_t s) {
+    if (n <= 0) return;
+    if (fp32)
+        k_cell_gather<float4><<<nblk(n, 256), 256, 0, s>>>((const float4 *)prel, perm, n,
+                                                           (float4 *)cpos);
+    else
+        k_cell_gather<double4><<<nblk(n, 256), 256, 0, s>>>((const double4 *)prel, perm, n,
+                                                            (double4 *)cpos);
 }
 
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
