@@ -65,6 +65,7 @@ struct _spme_t {
     // complete at ev_part[k]
     static constexpr int kOutParts = 4;
     cudaEvent_t ev_part[kOutParts] = {};
+    cudaEvent_t ev_in[kOutParts] = {};  // force part k uploaded
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int profiling = 0;  // 1: stage events; 2: events + real-space serialized
     cudaEvent_t ev[kStages + 1] = {};
@@ -450,6 +451,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_staged, cudaEventDisableTiming));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_stage_free, cudaEventDisableTiming));
     for (cudaEvent_t &ev : e->ev_part) TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    for (cudaEvent_t &ev : e->ev_in) TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     e->stream = e->own_stream;
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
     TRY_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
@@ -659,6 +661,8 @@ void destroy_impl(spme_t *e) {
     if (e->ev_stage_free) cudaEventDestroy(e->ev_stage_free);
     for (cudaEvent_t ev : e->ev_part)
         if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : e->ev_in)
+        if (ev) cudaEventDestroy(ev);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
     delete e;
 }
@@ -757,8 +761,10 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
     const bool prof = e->profiling;
     T *F = (T *)e->d_F, *W = (T *)e->d_W;
     if (prof) cudaEventRecord(e->ev[0], s);
-    spme::launch_pack_tiled<T>(f, ldf, n, R, F, s);
-    e->launches++;
+    if (f) {  // null: F already packed (host-pointer applies pack on the copy stream)
+        spme::launch_pack_tiled<T>(f, ldf, n, R, F, s);
+        e->launches++;
+    }
     if (prof) cudaEventRecord(e->ev[1], s);
     // the real-space sum runs before the mesh pipeline on the main stream, or
     // (overlap on) concurrently on the aux stream; at profiling level 2 always
@@ -956,26 +962,52 @@ int apply_impl(spme_t *e, int nrhs, double alpha, const void *f, long ldf, doubl
         char *up = (char *)u + el * (size_t)r0 * ldu;
         int st;
         if (mem == SPME_MEM_HOST) {
+            // With the mesh part and 8+ right-hand sides, forces go up and the result
+            // comes back in parts of rpart right-hand sides (a multiple of 4): the
+            // uploads run back to back on the copy stream and each part is packed on
+            // the main stream (after the position build) as it lands, and each result
+            // part is copied back while the next is interpolated
+            // (a direct pass: a captured graph would expose only its end; the
+            // launches it saves are negligible next to a pass of this size).
+            const int rpart = ((e->prm.terms & SPME_TERM_RECIP) && !e->profiling && R >= 8)
+                                  ? std::max(4, (R + spme_t::kOutParts - 1) / spme_t::kOutParts + 3) / 4 * 4
+                                  : 0;
             // stage the inputs on the copy stream (after the staging buffers' last
             // use), so the copy overlaps what the main stream is still running
             TRY_CUDA(cudaStreamWaitEvent(e->copy_stream, e->ev_stage_free, 0));
-            TRY_CUDA(cudaMemcpy2DAsync(e->d_fstage, row, fp, el * ldf, row, R,
-                                       cudaMemcpyHostToDevice, e->copy_stream));
+            if (rpart > 0) {
+                for (int q0 = 0, k = 0; q0 < R; q0 += rpart, k++) {
+                    const int q1 = std::min(R, q0 + rpart);
+                    char *fs = (char *)e->d_fstage + row * q0;
+                    TRY_CUDA(cudaMemcpy2DAsync(fs, row, fp + el * (size_t)q0 * ldf, el * ldf, row,
+                                               q1 - q0, cudaMemcpyHostToDevice, e->copy_stream));
+                    TRY_CUDA(cudaEventRecord(e->ev_in[k], e->copy_stream));
+                }
+            } else {
+                TRY_CUDA(cudaMemcpy2DAsync(e->d_fstage, row, fp, el * ldf, row, R,
+                                           cudaMemcpyHostToDevice, e->copy_stream));
+            }
             if (beta != 0.0)
                 TRY_CUDA(cudaMemcpy2DAsync(e->d_ustage, row, up, el * ldu, row, R,
                                            cudaMemcpyHostToDevice, e->copy_stream));
             TRY_CUDA(cudaEventRecord(e->ev_staged, e->copy_stream));
-            TRY_CUDA(cudaStreamWaitEvent(e->stream, e->ev_staged, 0));
-            // With the mesh part and 8+ right-hand sides the result leaves in parts
-            // (multiples of 4 right-hand sides), each copied on the copy stream while
-            // the next part is interpolated: a direct pass (a captured graph would
-            // expose only its end); the launches it saves are negligible next to a
-            // pass of this size.
-            const int rpart = ((e->prm.terms & SPME_TERM_RECIP) && !e->profiling && R >= 8)
-                                  ? std::max(4, (R + spme_t::kOutParts - 1) / spme_t::kOutParts + 3) / 4 * 4
-                                  : 0;
             if (rpart > 0) {
-                st = pass_body(e, R, e->d_fstage, 3L * n, e->d_ustage, 3L * n, alpha, beta, rpart);
+                for (int q0 = 0, k = 0; q0 < R; q0 += rpart, k++) {
+                    const int q1 = std::min(R, q0 + rpart);
+                    TRY_CUDA(cudaStreamWaitEvent(e->stream, e->ev_in[k], 0));
+                    if (is_fp32(e))
+                        spme::launch_pack_tiled<float>((const float *)e->d_fstage, 3L * n, n, R, q0,
+                                                       q1, (float *)e->d_F, e->stream);
+                    else
+                        spme::launch_pack_tiled<double>((const double *)e->d_fstage, 3L * n, n, R,
+                                                        q0, q1, (double *)e->d_F, e->stream);
+                    e->launches++;
+                }
+                TRY_CUDA(cudaGetLastError());
+            }
+            TRY_CUDA(cudaStreamWaitEvent(e->stream, e->ev_staged, 0));
+            if (rpart > 0) {
+                st = pass_body(e, R, nullptr, 3L * n, e->d_ustage, 3L * n, alpha, beta, rpart);
                 TRY(st);
                 for (int q0 = 0, k = 0; q0 < R; q0 += rpart, k++) {
                     const int q1 = std::min(R, q0 + rpart);

@@ -161,6 +161,9 @@ void launch_pack(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
 // both sides; W2 may be null (plain unpack).  Up to 48 KB of shared memory.
 template <typename T>
 void launch_pack_tiled(const T *f, long ld, int n, int R, T *F, cudaStream_t s);
+// (right-hand sides [r0, r1) of f into their columns of F[n][3R])
+template <typename T>
+void launch_pack_tiled(const T *f, long ld, int n, int R, int r0, int r1, T *F, cudaStream_t s);
 // (launch_unpack_tiled: right-hand sides [r0, r1) of the R in W / W2.)
 template <typename T>
 void launch_unpack_tiled(const T *W, const T *W2, int n, int R, int r0, int r1, double alpha,

@@ -62,21 +62,22 @@ constexpr int kPB = 32;
 
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_pack_tiled(const T *__restrict__ f, long ld, int n, int R, int pb, T *__restrict__ F) {
+k_pack_tiled(const T *__restrict__ f, long ld, int n, int R, int r0, int r1, int pb,
+             T *__restrict__ F) {
     extern __shared__ __align__(16) unsigned char pk_raw[];
-    T *tile = reinterpret_cast<T *>(pk_raw);  // [pb][C + 1]
-    const int C = 3 * R, CS = C + 1;
+    T *tile = reinterpret_cast<T *>(pk_raw);  // [pb][CP + 1]
+    const int C = 3 * R, CP = 3 * (r1 - r0), CS = CP + 1;  // row stride, columns written
     for (int i0 = blockIdx.x * pb; i0 < n; i0 += gridDim.x * pb) {
         const int np = min(pb, n - i0);
-        for (int t = threadIdx.x; t < R * 3 * np; t += blockDim.x) {
+        for (int t = threadIdx.x; t < (r1 - r0) * 3 * np; t += blockDim.x) {
             const int r = t / (3 * np), q = t - r * 3 * np;
             const int p = q / 3, d = q - p * 3;
-            tile[p * CS + 3 * r + d] = f[(size_t)r * ld + (size_t)3 * i0 + q];
+            tile[p * CS + 3 * r + d] = f[(size_t)(r0 + r) * ld + (size_t)3 * i0 + q];
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < np * C; t += blockDim.x) {
-            const int p = t / C, c = t - p * C;
-            F[(size_t)(i0 + p) * C + c] = tile[p * CS + c];
+        for (int t = threadIdx.x; t < np * CP; t += blockDim.x) {
+            const int p = t / CP, c = t - p * CP;
+            F[(size_t)(i0 + p) * C + 3 * r0 + c] = tile[p * CS + c];
         }
         __syncthreads();
     }
@@ -162,10 +163,15 @@ int tile_particles(int R, size_t elem) {
 
 template <typename T>
 void launch_pack_tiled(const T *f, long ld, int n, int R, T *F, cudaStream_t s) {
-    if (n <= 0 || R <= 0) return;
-    const int pb = tile_particles(R, sizeof(T));
-    const size_t smem = (size_t)pb * (3 * R + 1) * sizeof(T);
-    k_pack_tiled<T><<<tiled_blocks(n, pb), 256, smem, s>>>(f, ld, n, R, pb, F);
+    launch_pack_tiled<T>(f, ld, n, R, 0, R, F, s);
+}
+
+template <typename T>
+void launch_pack_tiled(const T *f, long ld, int n, int R, int r0, int r1, T *F, cudaStream_t s) {
+    if (n <= 0 || R <= 0 || r0 < 0 || r1 > R || r0 >= r1) return;
+    const int pb = tile_particles(r1 - r0, sizeof(T));
+    const size_t smem = (size_t)pb * (3 * (r1 - r0) + 1) * sizeof(T);
+    k_pack_tiled<T><<<tiled_blocks(n, pb), 256, smem, s>>>(f, ld, n, R, r0, r1, pb, F);
 }
 
 template <typename T>
@@ -190,6 +196,10 @@ void launch_self(const T *F, int n, int R, double self_c, T *W, cudaStream_t s) 
 
 template void launch_pack_tiled<float>(const float *, long, int, int, float *, cudaStream_t);
 template void launch_pack_tiled<double>(const double *, long, int, int, double *, cudaStream_t);
+template void launch_pack_tiled<float>(const float *, long, int, int, int, int, float *,
+                                       cudaStream_t);
+template void launch_pack_tiled<double>(const double *, long, int, int, int, int, double *,
+                                        cudaStream_t);
 template void launch_unpack_tiled<float>(const float *, const float *, int, int, int, int, double,
                                          double, float *, long, cudaStream_t);
 template void launch_unpack_tiled<double>(const double *, const double *, int, int, int, int,
