@@ -264,7 +264,7 @@ def test_fused_zfft_large_k_matches_3d_fft(gpu_lib, K, prec, tol):
     assert relerr(out[1], out[0]) < tol
 
 
-@pytest.mark.parametrize("R", [8, 12, 16])
+@pytest.mark.parametrize("R", [8, 10, 12, 16])
 def test_host_apply_in_parts_matches_device(gpu_lib, R):
     """Host-buffer applies with 8+ right-hand sides copy the result out in parts of
     4 right-hand sides while the next part is interpolated; the values are those of
