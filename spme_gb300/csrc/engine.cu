@@ -279,6 +279,87 @@ int alloc_tiles(spme_t *e) {
     return SPME_OK;
 }
 
+// cuFFT plan candidates: the default kernels and the patient-JIT search, which
+// is faster at some sizes and slower at others on GB300 (2D transforms at
+// K = 256: 2.44 vs 2.56 ms per direction; K = 160: 0.84 vs 0.80 ms).
+struct PlanCand {
+    cufftHandle h[2] = {0, 0};  // [patient]
+    size_t ws = 0;
+    void drop() {
+        for (cufftHandle &x : h)
+            if (x) {
+                cufftDestroy(x);
+                x = 0;
+            }
+    }
+};
+
+// Creates the candidates (patient one only when `both`); false if the default
+// plan cannot be made.
+bool make_cands(PlanCand &pc, int rank, int *n, int *inembed, int idist, int *onembed, int odist,
+                cufftType type, int batch, bool both) {
+    for (int pt = 0; pt < (both ? 2 : 1); pt++) {
+        cufftHandle h = 0;
+        if (cufftCreate(&h) != CUFFT_SUCCESS) continue;
+        bool ok = cufftSetAutoAllocation(h, 0) == CUFFT_SUCCESS;
+        if (ok && pt)
+            ok = cufftSetPlanPropertyInt64(h, NVFFT_PLAN_PROPERTY_INT64_PATIENT_JIT, 1) ==
+                 CUFFT_SUCCESS;
+        size_t w = 0;
+        if (ok)
+            ok = cufftMakePlanMany(h, rank, n, inembed, 1, idist, onembed, 1, odist, type, batch,
+                                   &w) == CUFFT_SUCCESS;
+        if (!ok) {
+            cufftDestroy(h);
+            continue;
+        }
+        pc.h[pt] = h;
+        pc.ws = std::max(pc.ws, w);
+    }
+    return pc.h[0] != 0;
+}
+
+// With the work area in place: times each candidate once (one warm and one
+// timed run on the engine's mesh buffers, whose contents the next pass
+// overwrites; not while the stream is being captured), keeps the faster.
+cufftHandle pick_cand(spme_t *e, PlanCand &pc, bool inverse) {
+    for (cufftHandle h : pc.h)
+        if (h) {
+            cufftSetWorkArea(h, e->d_work);
+            cufftSetStream(h, e->stream);
+        }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(e->stream, &cs);
+    auto exec = [&](cufftHandle h) {
+        if (is_fp32(e))
+            return inverse ? cufftExecC2R(h, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh)
+                           : cufftExecR2C(h, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh);
+        return inverse ? cufftExecZ2D(h, (cufftDoubleComplex *)e->d_cmesh, (cufftDoubleReal *)e->d_mesh)
+                       : cufftExecD2Z(h, (cufftDoubleReal *)e->d_mesh, (cufftDoubleComplex *)e->d_cmesh);
+    };
+    auto time_ms = [&](cufftHandle h) -> float {
+        if (exec(h) != CUFFT_SUCCESS) return -1.f;
+        cudaEventRecord(e->ev[0], e->stream);
+        if (exec(h) != CUFFT_SUCCESS) return -1.f;
+        cudaEventRecord(e->ev[1], e->stream);
+        float ms = -1.f;
+        if (cudaEventSynchronize(e->ev[1]) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]) != cudaSuccess)
+            return -1.f;
+        return ms;
+    };
+    int k = 0;
+    if (pc.h[1] && cs == cudaStreamCaptureStatusNone) {
+        const float t0 = time_ms(pc.h[0]), t1 = time_ms(pc.h[1]);
+        if (t1 > 0.f && t0 > 0.f && t1 < t0) k = 1;
+    }
+    cudaGetLastError();
+    const cufftHandle h = pc.h[k];
+    if (pc.h[1 - k]) cufftDestroy(pc.h[1 - k]);
+    pc.h[0] = pc.h[1] = 0;
+    return h;
+}
+
 int get_plans(spme_t *e, int C, PlanPair **out) {
     for (PlanPair &p : e->plans)
         if (p.C == C) {
@@ -290,139 +371,59 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
     PlanPair pp;
     pp.C = C;
     pp.maps_tile[0] = pp.maps_tile[1] = pp.maps_tile[2] = 0;
-    size_t ws1 = 0, ws2 = 0;
-    TRY_FFT(cufftCreate(&pp.fwd));
-    TRY_FFT(cufftCreate(&pp.bwd));
-    TRY_FFT(cufftSetAutoAllocation(pp.fwd, 0));
-    TRY_FFT(cufftSetAutoAllocation(pp.bwd, 0));
     cufftType tf = is_fp32(e) ? CUFFT_R2C : CUFFT_D2Z;
     cufftType tb = is_fp32(e) ? CUFFT_C2R : CUFFT_Z2D;
-    // component-major: batch b of the real mesh at b*K^3, of the half spectrum at b*Kc
+    // component-major: batch b of the real mesh at b*K^3, of the half spectrum at b*Kc.
+    // 3D plans (run in fft_mode 0, candidates timed there) and, in fft_mode 1, 2D
+    // (y, x) plans of the C*K z-planes with the same memory layout
     const long long K3 = (long long)K * K * K, Kc = (long long)K * K * (K / 2 + 1);
-    TRY_FFT(cufftMakePlanMany(pp.fwd, 3, n, re, 1, (int)K3, ce, 1, (int)Kc, tf, C, &ws1));
-    TRY_FFT(cufftMakePlanMany(pp.bwd, 3, n, ce, 1, (int)Kc, re, 1, (int)K3, tb, C, &ws2));
-    size_t ws = std::max(ws1, ws2);
+    const bool mode0 = e->fft_mode == 0, mode1 = e->fft_mode == 1;
+    PlanCand c3[2], c2[2];
+    auto drop_all = [&]() {
+        for (PlanCand &c : c3) c.drop();
+        for (PlanCand &c : c2) c.drop();
+    };
+    if (!make_cands(c3[0], 3, n, re, (int)K3, ce, (int)Kc, tf, C, mode0) ||
+        !make_cands(c3[1], 3, n, ce, (int)Kc, re, (int)K3, tb, C, mode0)) {
+        drop_all();
+        return SPME_ERR_CUDA;
+    }
+    const int Khp = K / 2 + 1, P2 = K * K, C2 = K * Khp;
+    int n2[2] = {K, K}, re2[2] = {K, K}, ce2[2] = {K, Khp};
+    if (mode1 && (!make_cands(c2[0], 2, n2, re2, P2, ce2, C2, tf, C * K, true) ||
+                  !make_cands(c2[1], 2, n2, ce2, C2, re2, P2, tb, C * K, true))) {
+        drop_all();
+        return SPME_ERR_CUDA;
+    }
+    size_t ws = 0;
+    for (PlanCand &c : c3) ws = std::max(ws, c.ws);
+    for (PlanCand &c : c2) ws = std::max(ws, c.ws);
     if (ws > e->work_bytes) {
         dfree(e->d_work);
         e->d_work = nullptr;
         e->work_bytes = 0;
-        TRY(dalloc(&e->d_work, ws));
+        if (dalloc(&e->d_work, ws) != SPME_OK) {
+            drop_all();
+            return SPME_ERR_NOMEM;
+        }
         e->work_bytes = ws;
         for (PlanPair &q : e->plans) {
             TRY_FFT(cufftSetWorkArea(q.fwd, e->d_work));
             TRY_FFT(cufftSetWorkArea(q.bwd, e->d_work));
+            if (q.has2d) {
+                TRY_FFT(cufftSetWorkArea(q.fwd2, e->d_work));
+                TRY_FFT(cufftSetWorkArea(q.bwd2, e->d_work));
+            }
         }
     }
-    TRY_FFT(cufftSetWorkArea(pp.fwd, e->d_work));
-    TRY_FFT(cufftSetWorkArea(pp.bwd, e->d_work));
-    TRY_FFT(cufftSetStream(pp.fwd, e->stream));
-    TRY_FFT(cufftSetStream(pp.bwd, e->stream));
-    if (e->fft_mode == 1) {
-        // 2D (y, x) transforms of the C*K z-planes: same memory layout as the
-        // 3D transform's first two stages.  Two candidates per direction, cuFFT's
-        // default kernels and its patient-JIT search, which is faster at some sizes
-        // and slower at others on GB300 (K = 256: 2.44 vs 2.56 ms per direction;
-        // K = 160: 0.84 vs 0.80 ms); both are timed once and the faster is kept.
-        const int Khp = K / 2 + 1;
-        int n2[2] = {K, K}, re2[2] = {K, K}, ce2[2] = {K, Khp};
-        const int P2 = K * K, C2 = K * Khp;
-        cufftHandle cand[2][2] = {{0, 0}, {0, 0}};  // [inverse][patient]
-        auto drop = [&]() {
-            for (auto &row : cand)
-                for (cufftHandle &h : row)
-                    if (h) cufftDestroy(h);
-        };
-        size_t ws2d = 0;
-        for (int d = 0; d < 2; d++)
-            for (int pt = 0; pt < 2; pt++) {
-                cufftHandle h = 0;
-                if (cufftCreate(&h) != CUFFT_SUCCESS) continue;
-                bool ok = cufftSetAutoAllocation(h, 0) == CUFFT_SUCCESS;
-                if (ok && pt)
-                    ok = cufftSetPlanPropertyInt64(h, NVFFT_PLAN_PROPERTY_INT64_PATIENT_JIT, 1) ==
-                         CUFFT_SUCCESS;
-                size_t w = 0;
-                if (ok)
-                    ok = (d == 0 ? cufftMakePlanMany(h, 2, n2, re2, 1, P2, ce2, 1, C2, tf, C * K, &w)
-                                 : cufftMakePlanMany(h, 2, n2, ce2, 1, C2, re2, 1, P2, tb, C * K,
-                                                     &w)) == CUFFT_SUCCESS;
-                if (!ok) {
-                    cufftDestroy(h);
-                    continue;
-                }
-                cand[d][pt] = h;
-                ws2d = std::max(ws2d, w);
-            }
-        if (!cand[0][0] || !cand[1][0]) {
-            drop();
-            return SPME_ERR_CUDA;
-        }
-        if (ws2d > e->work_bytes) {
-            dfree(e->d_work);
-            e->d_work = nullptr;
-            e->work_bytes = 0;
-            if (dalloc(&e->d_work, ws2d) != SPME_OK) {
-                drop();
-                return SPME_ERR_NOMEM;
-            }
-            e->work_bytes = ws2d;
-            for (PlanPair &q : e->plans) {
-                TRY_FFT(cufftSetWorkArea(q.fwd, e->d_work));
-                TRY_FFT(cufftSetWorkArea(q.bwd, e->d_work));
-                if (q.has2d) {
-                    TRY_FFT(cufftSetWorkArea(q.fwd2, e->d_work));
-                    TRY_FFT(cufftSetWorkArea(q.bwd2, e->d_work));
-                }
-            }
-            TRY_FFT(cufftSetWorkArea(pp.fwd, e->d_work));
-            TRY_FFT(cufftSetWorkArea(pp.bwd, e->d_work));
-        }
-        for (auto &row : cand)
-            for (cufftHandle h : row)
-                if (h) {
-                    cufftSetWorkArea(h, e->d_work);
-                    cufftSetStream(h, e->stream);
-                }
-        // time each direction's candidates (one warm and one timed run on the
-        // engine's mesh buffers, whose contents the next pass overwrites); not
-        // while the stream is being captured
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(e->stream, &cs);
-        auto exec = [&](cufftHandle h, int d) {
-            if (is_fp32(e))
-                return d == 0 ? cufftExecR2C(h, (cufftReal *)e->d_mesh, (cufftComplex *)e->d_cmesh)
-                              : cufftExecC2R(h, (cufftComplex *)e->d_cmesh, (cufftReal *)e->d_mesh);
-            return d == 0 ? cufftExecD2Z(h, (cufftDoubleReal *)e->d_mesh,
-                                         (cufftDoubleComplex *)e->d_cmesh)
-                          : cufftExecZ2D(h, (cufftDoubleComplex *)e->d_cmesh,
-                                         (cufftDoubleReal *)e->d_mesh);
-        };
-        auto time_ms = [&](cufftHandle h, int d) -> float {
-            if (exec(h, d) != CUFFT_SUCCESS) return -1.f;
-            cudaEventRecord(e->ev[0], e->stream);
-            if (exec(h, d) != CUFFT_SUCCESS) return -1.f;
-            cudaEventRecord(e->ev[1], e->stream);
-            float ms = -1.f;
-            if (cudaEventSynchronize(e->ev[1]) != cudaSuccess ||
-                cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]) != cudaSuccess)
-                return -1.f;
-            return ms;
-        };
-        cufftHandle pick[2];
-        for (int d = 0; d < 2; d++) {
-            int k = 0;
-            if (cand[d][1] && cs == cudaStreamCaptureStatusNone) {
-                const float t0 = time_ms(cand[d][0], d), t1 = time_ms(cand[d][1], d);
-                if (t1 > 0.f && t0 > 0.f && t1 < t0) k = 1;
-            }
-            pick[d] = cand[d][k];
-            if (cand[d][1 - k]) cufftDestroy(cand[d][1 - k]);
-        }
-        TRY_CUDA(cudaGetLastError());
-        pp.fwd2 = pick[0];
-        pp.bwd2 = pick[1];
+    pp.fwd = pick_cand(e, c3[0], false);
+    pp.bwd = pick_cand(e, c3[1], true);
+    if (mode1) {
+        pp.fwd2 = pick_cand(e, c2[0], false);
+        pp.bwd2 = pick_cand(e, c2[1], true);
         pp.has2d = true;
     }
+    TRY_CUDA(cudaGetLastError());
     e->plans.push_back(pp);
     *out = &e->plans.back();
     return SPME_OK;
