@@ -832,7 +832,7 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
             TRY_CUDA(spme::launch_zfft_influence<T>(e->zmap, (T *)e->d_cmesh, (const T *)e->d_tab,
                                                     (const T *)e->d_ztw, e->d_zip, e->zp,
                                                     e->prm.box_size, R, e->d_err, s));
-            e->launches += 2;
+            e->launches++;
         } else {
             spme::launch_influence<T>((T *)e->d_cmesh, (const T *)e->d_tab, K, e->prm.box_size,
                                       R, s);

@@ -27,9 +27,11 @@
 // covers it).
 //
 // The reference's Nyquist convention (influence.cu) needs the Hermitian part
-// on the kx = 0 and (even K) kx = K/2 planes: pairing (ky, kz) with
-// (-ky, -kz) before the inverse z-transform equals pairing (ky, z) with
-// (-ky, z) after it, which k_hermitian_xplanes does on those two planes.
+// of the influenced spectrum on the kx = 0 and (even K) kx = K/2 planes.  The
+// forward spectrum of real data is Hermitian there, and for Hermitian g the
+// Hermitian part of I(k) g equals (I(k) + I(-k))/2 g: the kernel applies that
+// averaged tensor on those planes (I(-k) differs from I(k) only in the sign of
+// the couplings between a Nyquist and a non-Nyquist axis, which cancel).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -380,6 +382,12 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__
     const int ky = valid ? fl / Kh : 0, kx = valid ? fl - ky * Kh : 0;
     const T kxv = (T)kx * twopi_L;  // kx <= K/2: non-negative wavenumber
     const T kyv = (T)(ky <= K / 2 ? ky : ky - K) * twopi_L;
+    // kx = 0 and (even K) K/2 planes hold k and -k: there the tensor is averaged
+    // with its mirror (the Hermitian part of the result):
+    // with s_i = +1 for a zero or Nyquist index and -1 otherwise, the ij
+    // coupling survives when s_i s_j = +1 (s_x = +1 on these planes)
+    const bool xplane = valid && (kx == 0 || (!(K & 1) && kx == K / 2));
+    const bool sy = ky == 0 || (!(K & 1) && ky == K / 2);
     T m2r[MAXP], cr[MAXP];
 #pragma unroll
     for (int i = 0; i < MAXP; i++) {
@@ -416,8 +424,14 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__
                 const int kz = perm[p];
                 const T kzv = (T)(kz <= K / 2 ? kz : kz - K) * twopi_L;
                 const T m2 = m2r[i], c = cr[i];
-                const T b0 = m2 - c * kxv * kxv, b1 = -c * kxv * kyv, b2 = -c * kxv * kzv;
-                const T b3 = m2 - c * kyv * kyv, b4 = -c * kyv * kzv, b5 = m2 - c * kzv * kzv;
+                T b1 = -c * kxv * kyv, b2 = -c * kxv * kzv, b4 = -c * kyv * kzv;
+                if (xplane) {
+                    const bool sz = kz == 0 || (!(K & 1) && kz == K / 2);
+                    if (!sy) b1 = T(0);
+                    if (!sz) b2 = T(0);
+                    if (sy != sz) b4 = T(0);
+                }
+                const T b0 = m2 - c * kxv * kxv, b3 = m2 - c * kyv * kyv, b5 = m2 - c * kzv * kzv;
                 Cx<T> *q0 = B + (size_t)p * W + wi;
                 Cx<T> *q1 = q0 + GS;
                 Cx<T> *q2 = q1 + GS;
@@ -433,38 +447,6 @@ k_zfft_influence(const __grid_constant__ CUtensorMap gmap, const T *__restrict__
         // hand the buffer to the TMA warp (its store reads what this thread wrote)
         fence_proxy_async();
         mbar_arrive(&done[b]);
-    }
-}
-
-// Hermitian part over (ky, z) <-> (-ky, z) on the kx = 0 and (even K) kx = K/2
-// planes, after the inverse z-transform.
-template <typename T>
-__global__ void k_hermitian_xplanes(Cx<T> *__restrict__ G, int K, int C) {
-    const int Khp = K / 2 + 1;
-    const int Kh = K / 2 + 1;
-    const int nplanes = (K & 1) ? 1 : 2;
-    const size_t total = (size_t)C * nplanes * K * Kh;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const int y = (int)(t % Kh);
-        size_t rest = t / Kh;
-        const int z = (int)(rest % K);
-        rest /= K;
-        const int pl = (int)(rest % nplanes);
-        const size_t c = rest / nplanes;
-        const int x = pl ? K / 2 : 0;
-        const int y2 = (K - y) % K;
-        const size_t zrow = (c * K + z) * K;
-        Cx<T> *a = G + (zrow + y) * Khp + x;
-        if (y == y2) {
-            a->im = T(0);
-            continue;
-        }
-        Cx<T> *bb = G + (zrow + y2) * Khp + x;
-        const Cx<T> oa = *a, ob = *bb;
-        const Cx<T> h = {T(0.5) * (oa.re + ob.re), T(0.5) * (oa.im - ob.im)};
-        *a = h;
-        *bb = {h.re, -h.im};
     }
 }
 
@@ -621,7 +603,8 @@ template <typename T>
 cudaError_t launch_zfft_influence(const CUtensorMap &map, T *G, const T *tab2, const T *tw,
                                   const int *perm, const ZPlan &zp, double L, int R, int *err,
                                   cudaStream_t s) {
-    const int K = zp.K, Kh = K / 2 + 1;
+    (void)G;  // addressed through the tensor map
+    const int K = zp.K;
     const int ci = zcfg_index(K, sizeof(T));
     if (ci < 0) return cudaErrorInvalidValue;
     const T twopi_L = (T)(2.0 * M_PI / L);
@@ -644,12 +627,7 @@ cudaError_t launch_zfft_influence(const CUtensorMap &map, T *G, const T *tab2, c
         SPME_ZCFG(1, 192, 1, 24)
     }
 #undef SPME_ZCFG
-    if (e != cudaSuccess) return e;
-    const int nplanes = (K & 1) ? 1 : 2;
-    const size_t work = (size_t)3 * R * nplanes * K * Kh;
-    const int blocks = (int)std::min<size_t>((work + 255) / 256, 152 * 8);
-    k_hermitian_xplanes<T><<<blocks, 256, 0, s>>>(reinterpret_cast<Cx<T> *>(G), K, 3 * R);
-    return cudaGetLastError();
+    return e;
 }
 
 template cudaError_t launch_zfft_influence<float>(const CUtensorMap &, float *, const float *,
