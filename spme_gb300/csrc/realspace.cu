@@ -152,6 +152,10 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
     __shared__ G nb_shift[27][3];
     __shared__ G cx[kCap], cy[kCap], cz[kCap];
     __shared__ int cj[kCap];
+    // FP64 engines: FP32 copies for a conservative first distance test (the FP64
+    // test then runs only on candidates that pass it)
+    constexpr bool kPre = sizeof(G) == 8;
+    __shared__ float fx[kPre ? kCap : 1], fy[kPre ? kCap : 1], fz[kPre ? kCap : 1];
     __shared__ int hits[kWarps][64];
     // one record per buffered pair: unit vector and F in one 16/32-byte vector,
     // then G and the start of the partner's force row
@@ -197,10 +201,19 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
             cy[q] = p.y + nb_shift[k][1];
             cz[q] = p.z + nb_shift[k][2];
             cj[q] = cell_perm[js];
+            if constexpr (kPre) {
+                fx[q] = (float)cx[q];
+                fy[q] = (float)cy[q];
+                fz[q] = (float)cz[q];
+            }
         }
     }
     __syncthreads();
     const bool single = nc < 3;
+    // the FP32 test accepts a superset of the pairs within rc: coordinates lie
+    // within 3 cells, so FP32 rounding moves d^2 by far less than the margin
+    const bool pre = kPre && staged && !single;
+    const float pre_r2 = (float)((double)rc2 * 1.0001 + 1e-5 * 9.0 * (double)h * (double)h);
     const G invL = G(1) / L;
     const int ib0 = cell_off[cell], ie = cell_off[cell + 1];
 
@@ -287,7 +300,13 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
             for (int q0 = 0; q0 < ncand; q0 += 32) {
                 const int q = q0 + lane;
                 bool hit = false;
-                if (q < ncand) {
+                bool maybe = q < ncand;
+                if (pre && maybe) {
+                    const float e0 = (float)pi.x - fx[q], e1 = (float)pi.y - fy[q],
+                                e2 = (float)pi.z - fz[q];
+                    maybe = e0 * e0 + e1 * e1 + e2 * e2 < pre_r2;
+                }
+                if (maybe) {
                     G x, y, z;
                     int j;
                     candidate(q, x, y, z, j);
