@@ -54,13 +54,12 @@ __global__ void k_unpack(const T *__restrict__ W, int n, int R, T alpha, T beta,
     }
 }
 
-// Tiled forms: a block moves pb particles at a time (at most 32, fewer for very
+// Tiled forms: a block moves pb particles at a time (at most kPB, fewer for
 // many right-hand sides so the tile stays within 48 KB) through shared memory
 // so both sides are coalesced (rows of 3 pb values per right-hand side on the
-// caller's side, rows of C values per particle on the packed side).
-// particles per shared-memory tile (at most; 48 KB caps it for many components):
-// 128 measured faster than 32 for the 48-component pack/unpack at N = 1e6
-// (0.157 / 0.158 vs 0.172 / 0.178 ms)
+// caller's side, rows of C values per particle on the packed side).  128
+// measured faster than 32 for the 48-component pack/unpack at N = 1e6 (0.157 /
+// 0.158 vs 0.172 / 0.178 ms).
 constexpr int kPB = 128;
 
 template <typename T>
