@@ -407,13 +407,17 @@ int get_plans(spme_t *e, int C, PlanPair **out) {
             return SPME_ERR_NOMEM;
         }
         e->work_bytes = ws;
+        bool ok = true;
         for (PlanPair &q : e->plans) {
-            TRY_FFT(cufftSetWorkArea(q.fwd, e->d_work));
-            TRY_FFT(cufftSetWorkArea(q.bwd, e->d_work));
-            if (q.has2d) {
-                TRY_FFT(cufftSetWorkArea(q.fwd2, e->d_work));
-                TRY_FFT(cufftSetWorkArea(q.bwd2, e->d_work));
-            }
+            ok = ok && cufftSetWorkArea(q.fwd, e->d_work) == CUFFT_SUCCESS &&
+                 cufftSetWorkArea(q.bwd, e->d_work) == CUFFT_SUCCESS;
+            if (q.has2d)
+                ok = ok && cufftSetWorkArea(q.fwd2, e->d_work) == CUFFT_SUCCESS &&
+                     cufftSetWorkArea(q.bwd2, e->d_work) == CUFFT_SUCCESS;
+        }
+        if (!ok) {
+            drop_all();
+            return SPME_ERR_CUDA;
         }
     }
     pp.fwd = pick_cand(e, c3[0], false);
