@@ -64,3 +64,22 @@ def test_xyz_errors(tmp_path):
         spme_gb300.read_xyz(str(bad))
     with pytest.raises(spme_gb300.SpmeError):
         spme_gb300.read_xyz(str(tmp_path / "missing.xyz"))
+
+
+def test_autotune_cache_key_and_round_trip(tmp_path, monkeypatch):
+    """The tile autotuner's cache: keys round N up to a power of two and carry the
+    rest of the configuration; the file survives a save/load round trip, and an
+    unreadable file reads as empty."""
+    from spme_gb300 import autotune as at
+    k1 = at.config_key("GB300", 1_000_000, 256, 6, 16, "fp32", 7)
+    assert k1 == "GB300|N1048576|K256|p6|R16|fp32|t7"
+    assert at.config_key("GB300", 600_000, 256, 6, 16, "fp32", 7) == k1
+    assert at.config_key("GB300", 1_000_000, 256, 6, 8, "fp32", 7) != k1
+    path = tmp_path / "sub" / "autotune.json"
+    monkeypatch.setenv("SPME_AUTOTUNE_CACHE", str(path))
+    assert at.cache_path() == str(path)
+    assert at._load_cache(str(path)) == {}
+    at._save_cache(str(path), {k1: [16, 8, 4]})
+    assert at._load_cache(str(path)) == {k1: [16, 8, 4]}
+    path.write_text("{not json")
+    assert at._load_cache(str(path)) == {}
