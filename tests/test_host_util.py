@@ -83,3 +83,29 @@ def test_autotune_cache_key_and_round_trip(tmp_path, monkeypatch):
     assert at._load_cache(str(path)) == {k1: [16, 8, 4]}
     path.write_text("{not json")
     assert at._load_cache(str(path)) == {}
+
+
+def test_uneven_batch_systems():
+    """The uneven-batch workload: N log-uniform in [500, 50000], L for volume
+    fraction 0.05, K the smallest 5-smooth size >= 0.6 L (and >= p), p in {4, 6, 8},
+    the same list for the same seed."""
+    import math
+
+    from spme_gb300.batch import uneven_systems
+
+    def smooth(k):
+        for q in (2, 3, 5):
+            while k % q == 0:
+                k //= q
+        return k == 1
+
+    sys_a = uneven_systems(count=64, seed=1234)
+    assert sys_a == uneven_systems(count=64, seed=1234)
+    assert sys_a != uneven_systems(count=64, seed=99)
+    assert len(sys_a) == 64
+    for s in sys_a:
+        assert 500 <= s["N"] <= 50_000
+        assert math.isclose(s["L"], (s["N"] * 4.0 / 3.0 * math.pi / 0.05) ** (1.0 / 3.0))
+        assert s["p"] in (4, 6, 8)
+        assert smooth(s["K"]) and s["K"] >= max(0.6 * s["L"], s["p"])
+        assert not any(smooth(k) for k in range(math.ceil(0.6 * s["L"]), s["K"])) or s["K"] == s["p"]
