@@ -182,13 +182,16 @@ void spme_free(void *p);
  * work ordered on `stream` (NULL: the legacy default stream):
  *   u_r = beta*u_r + alpha * (M_real + M_self) f_r,  layout v[r*ld + 3i + d],
  * with the same Beenakker real-space sum and self term as spme_apply.
- * Scratch is one fixed device array inside the library (about 16 MB, held on
- * every GPU that loads the library until exit), so the sizes are capped:
- * np <= SPME_NOALLOC_MAX_NP, nrhs <= SPME_NOALLOC_MAX_NRHS; larger requests
- * return SPME_ERR_TOO_LARGE.  All calls share that array: calls that overlap
- * on the GPU race and must be serialised by the caller.  The first call on a
- * device looks up the array's device address; make it before any stream
- * capture. */
+ * Scratch is one fixed device array inside the library (about 16 MB), so the
+ * sizes are capped: np <= SPME_NOALLOC_MAX_NP, nrhs <= SPME_NOALLOC_MAX_NRHS;
+ * larger requests return SPME_ERR_TOO_LARGE.  The array takes device memory on
+ * a device when the first call there loads the library's code (CUDA loads it
+ * lazily) and keeps it until the process exits: make one call, a zero-size one
+ * (np = 0) is enough, on each device before reserving the rest of its memory
+ * and before any stream capture.  Resetting the device after that call is not
+ * supported.  All calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  A pending error of the caller's earlier
+ * launches is cleared on entry; the status describes this call only. */
 #define SPME_NOALLOC_MAX_NP 65536
 #define SPME_NOALLOC_MAX_NRHS 4
 int spme_realspace_apply_noalloc(int np, const double *pos, double box_size, double xi,

@@ -9,16 +9,28 @@
 //
 // Limits (also in include/spme_gb300.h): np <= SPME_NOALLOC_MAX_NP, nrhs <=
 // SPME_NOALLOC_MAX_NRHS, at most kMaxCells real-space cells (the cell count is
-// capped, which only makes cells larger).  Every GPU that loads the library
-// holds the array (kScratchBytes) until the process exits.
+// capped, which only makes cells larger).
+//
+// When the array takes device memory: CUDA loads this file's module on a
+// device lazily (the default module loading), at the first use of one of its
+// kernels or symbols there, and the array (kScratchBytes) is allocated then
+// and held until the process exits.  The first call on each device, a
+// zero-size one included, looks up the array's address with that device
+// current and so loads the module: a caller that reserves all remaining device
+// memory for its own pool makes one call (np = 0 is enough) before doing so,
+// and before any stream capture.  The address is kept per device for the
+// process; resetting a device (cudaDeviceReset) after that first call is not
+// supported.
 //
 // Every call shares the one array, which keeps the previous call's contents:
 // the cell counts are cleared at the start of each call, everything else is
 // overwritten before it is read.  Calls whose work overlaps on the GPU (two
 // streams, or two host threads) race on the array and give wrong results;
-// serialise them.  The first call on each device looks up the array's device
-// address with that device current; make that first call before any stream
-// capture.
+// serialise them.
+//
+// Errors: a pending error from the caller's earlier, unrelated launches is
+// cleared on entry (cudaGetLastError), so the status returned describes this
+// call's own work only.
 #include <mutex>
 
 #include "kernels.h"
@@ -83,12 +95,15 @@ extern "C" int spme_realspace_apply_noalloc(int np, const double *pos, double bo
         !(rcut > 0.0 && rcut < 0.5 * box_size))
         return SPME_ERR_INVALID;
     if ((size_t)np > kMaxNp || nrhs > SPME_NOALLOC_MAX_NRHS) return SPME_ERR_TOO_LARGE;
-    if (np == 0 || nrhs == 0) return SPME_OK;
-    if (!pos || !f || !u || ldf < 3L * np || ldu < 3L * np) return SPME_ERR_INVALID;
-
+    // an error left pending by the caller's earlier launches is not this call's
+    cudaGetLastError();
+    // before the zero-size return: a zero-size first call loads the module (and
+    // with it the scratch array) on this device
     unsigned char *base = nullptr;
     int st = scratch_address(&base);
     if (st != SPME_OK) return st;
+    if (np == 0 || nrhs == 0) return SPME_OK;
+    if (!pos || !f || !u || ldf < 3L * np || ldu < 3L * np) return SPME_ERR_INVALID;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // cells of edge >= rc, at most kMaxNc per axis (fewer than 3 -> one cell)
