@@ -271,23 +271,55 @@ int oracle_recip(int np, const double *pos, double L, double xi, double a, int K
  * replacing the far-field form for r < 2a. */
 void oracle_real_FG(double r, double xi, double a, double *F, double *G)
 {
+    /* Beenakker's real-space RPY form divided by a; for r < 2a plus
+     * (overlap RPY - far-field RPY), whose 1/r and 1/r^3 terms cancel: there
+     * the sum is written with x = xi r, S(x) = erf(x)/x and
+     * psi(x) = (erf(x) - 2x e^{-x^2}/sqrt(pi))/x^3 (Maclaurin series below
+     * x = 0.5), which keeps full precision as r -> 0 and is finite at r = 0. */
+    static const double ser_s[10] = {1.0, -1.0 / 3, 1.0 / 10, -1.0 / 42, 1.0 / 216,
+                                     -1.0 / 1320, 1.0 / 9360, -1.0 / 75600,
+                                     1.0 / 685440, -1.0 / 6894720};
+    static const double ser_p[10] = {2.0 / 3, -2.0 / 5, 1.0 / 7, -1.0 / 27, 1.0 / 132,
+                                     -1.0 / 780, 1.0 / 5400, -1.0 / 42840,
+                                     1.0 / 383040, -1.0 / 3810240};
     const double rsp = 1.0 / sqrt(M_PI);
-    double xr = xi * r, e = exp(-xr * xr), ec = erfc(xr);
-    double r2 = r * r, a3 = a * a * a;
-    double xi2 = xi * xi, xi3 = xi2 * xi, xi5 = xi3 * xi2, xi7 = xi5 * xi2;
-    double f = ec * (0.75 * a / r + 0.5 * a3 / (r2 * r))
-               + e * rsp * (4.0 * xi7 * a3 * r2 * r2 + 3.0 * xi3 * a * r2 - 20.0 * xi5 * a3 * r2
-                            - 4.5 * xi * a + 14.0 * xi3 * a3 + xi * a3 / r2);
-    double g = ec * (0.75 * a / r - 1.5 * a3 / (r2 * r))
-               + e * rsp * (-4.0 * xi7 * a3 * r2 * r2 - 3.0 * xi3 * a * r2 + 16.0 * xi5 * a3 * r2
-                            + 1.5 * xi * a - 2.0 * xi3 * a3 - 3.0 * xi * a3 / r2);
+    double x = xi * r, x2 = x * x, e = exp(-x2);
     if (r < 2.0 * a) {
-        /* overlap RPY minus far-field RPY */
-        f += (1.0 - 9.0 * r / (32.0 * a)) - (0.75 * a / r + 0.5 * a3 / (r2 * r));
-        g += (3.0 * r / (32.0 * a)) - (0.75 * a / r - 1.5 * a3 / (r2 * r));
+        double S = 0.0, P = 0.0, x4 = x2 * x2, xi3a2 = xi * xi * xi * a * a;
+        int k;
+        if (x < 0.5) {
+            for (k = 9; k >= 0; k--) {
+                S = S * x2 + ser_s[k];
+                P = P * x2 + ser_p[k];
+            }
+            S *= 2.0 * rsp;
+            P *= 2.0 * rsp;
+        } else {
+            double ef = erf(x);
+            S = ef / x;
+            P = (ef - 2.0 * rsp * x * e) / (x2 * x);
+        }
+        *F = xi * (-0.75 * S + rsp * e * (3.0 * x2 - 4.5))
+             + xi3a2 * (-0.5 * P + rsp * e * (4.0 * x4 - 20.0 * x2 + 14.0))
+             + (1.0 - 9.0 * r / (32.0 * a)) / a;
+        *G = xi * (-0.75 * S + rsp * e * (1.5 - 3.0 * x2))
+             + xi3a2 * (1.5 * P + rsp * e * (-4.0 * x4 + 16.0 * x2 - 2.0))
+             + 3.0 * r / (32.0 * a * a);
+        return;
     }
-    *F = f / a;
-    *G = g / a;
+    {
+        double ec = erfc(x);
+        double r2 = r * r, a3 = a * a * a;
+        double xi2 = xi * xi, xi3 = xi2 * xi, xi5 = xi3 * xi2, xi7 = xi5 * xi2;
+        double f = ec * (0.75 * a / r + 0.5 * a3 / (r2 * r))
+                   + e * rsp * (4.0 * xi7 * a3 * r2 * r2 + 3.0 * xi3 * a * r2 - 20.0 * xi5 * a3 * r2
+                                - 4.5 * xi * a + 14.0 * xi3 * a3 + xi * a3 / r2);
+        double g = ec * (0.75 * a / r - 1.5 * a3 / (r2 * r))
+                   + e * rsp * (-4.0 * xi7 * a3 * r2 * r2 - 3.0 * xi3 * a * r2 + 16.0 * xi5 * a3 * r2
+                                + 1.5 * xi * a - 2.0 * xi3 * a3 - 3.0 * xi * a3 / r2);
+        *F = f / a;
+        *G = g / a;
+    }
 }
 
 double oracle_self_coeff(double xi, double a)
@@ -354,7 +386,8 @@ int oracle_real_self(int np, const double *pos, double L, double xi, double a, d
                             if (r2 >= rc2) continue;
                             rr = sqrt(r2);
                             oracle_real_FG(rr, xi, a, &F, &G);
-                            for (d = 0; d < 3; d++) dv[d] /= rr;
+                            /* coincident particles: no direction, the G term vanishes */
+                            for (d = 0; d < 3; d++) dv[d] = rr > 0.0 ? dv[d] / rr : 0.0;
                             for (r = 0; r < nrhs; r++) {
                                 const double *fj = f + r * ldf + 3 * j;
                                 double dot = dv[0] * fj[0] + dv[1] * fj[1] + dv[2] * fj[2];

@@ -24,24 +24,68 @@ __device__ __forceinline__ double d_erfc(double x) { return erfc(x); }
 __device__ __forceinline__ float d_exp(float x) { return expf(x); }
 __device__ __forceinline__ double d_exp(double x) { return exp(x); }
 
-// M_real(r) = F I + G rhat rhat, Beenakker's form divided by a, plus
-// (overlap RPY - far-field RPY) for r < 2a.
+__device__ __forceinline__ float d_erf(float x) { return erff(x); }
+__device__ __forceinline__ double d_erf(double x) { return erf(x); }
+
+// Maclaurin coefficients (without the 2/sqrt(pi) factor) of S(x) = erf(x)/x,
+// (-1)^n / (n! (2n+1)), and of psi(x) = (erf(x) - 2x e^{-x^2}/sqrt(pi)) / x^3,
+// (-1)^(n+1) 2n / (n! (2n+1)) for n >= 1; in x^2, ten terms (below 1e-17
+// relative for x < 0.5).
+__device__ __constant__ double kSerS[10] = {1.0, -1.0 / 3, 1.0 / 10, -1.0 / 42, 1.0 / 216,
+                                            -1.0 / 1320, 1.0 / 9360, -1.0 / 75600,
+                                            1.0 / 685440, -1.0 / 6894720};
+__device__ __constant__ double kSerPsi[10] = {2.0 / 3, -2.0 / 5, 1.0 / 7, -1.0 / 27, 1.0 / 132,
+                                              -1.0 / 780, 1.0 / 5400, -1.0 / 42840,
+                                              1.0 / 383040, -1.0 / 3810240};
+
+// M_real(r) = F I + G rhat rhat: Beenakker's real-space form divided by a, and
+// for r < 2a plus (overlap RPY - far-field RPY).  For r < 2a the 1/r and 1/r^3
+// terms of the two cancel; written with x = xi r, S(x) = erf(x)/x and psi(x)
+// they cancel analytically (no loss of precision as r -> 0, finite at r = 0):
+//   F = xi [-3/4 S + e (3x^2 - 9/2)/sqrt(pi)] + xi^3 a^2 [-psi/2 + e (4x^4 - 20x^2 + 14)/sqrt(pi)]
+//       + (1 - 9r/(32a)) / a
+//   G = xi [-3/4 S + e (3/2 - 3x^2)/sqrt(pi)] + xi^3 a^2 [3psi/2 + e (-4x^4 + 16x^2 - 2)/sqrt(pi)]
+//       + 3r/(32 a^2)
+// with e = exp(-x^2); S and psi from their series for x < 0.5.
 template <typename T>
 __device__ __forceinline__ void real_FG(T r, T xi, T a, T &F, T &G) {
     const T rsp = T(0.56418958354775628695);  // 1/sqrt(pi)
-    const T xr = xi * r, e = d_exp(-xr * xr), ec = d_erfc(xr);
+    const T x = xi * r, x2 = x * x, e = d_exp(-x2);
+    if (r < T(2) * a) {
+        T S, P;
+        if (x < T(0.5)) {
+            S = T(0);
+            P = T(0);
+#pragma unroll
+            for (int k = 9; k >= 0; k--) {
+                S = S * x2 + T(kSerS[k]);
+                P = P * x2 + T(kSerPsi[k]);
+            }
+            S *= T(2) * rsp;
+            P *= T(2) * rsp;
+        } else {
+            const T ef = d_erf(x);
+            S = ef / x;
+            P = (ef - T(2) * rsp * x * e) / (x2 * x);
+        }
+        const T x4 = x2 * x2, xi3a2 = xi * xi * xi * a * a;
+        F = xi * (T(-0.75) * S + rsp * e * (T(3) * x2 - T(4.5))) +
+            xi3a2 * (T(-0.5) * P + rsp * e * (T(4) * x4 - T(20) * x2 + T(14))) +
+            (T(1) - T(9) * r / (T(32) * a)) / a;
+        G = xi * (T(-0.75) * S + rsp * e * (T(1.5) - T(3) * x2)) +
+            xi3a2 * (T(1.5) * P + rsp * e * (T(-4) * x4 + T(16) * x2 - T(2))) +
+            T(3) * r / (T(32) * a * a);
+        return;
+    }
+    const T ec = d_erfc(x);
     const T r2 = r * r, a3 = a * a * a, ir = T(1) / r, ir3 = ir * ir * ir, ir2 = ir * ir;
     const T xi2 = xi * xi, xi3 = xi2 * xi, xi5 = xi3 * xi2, xi7 = xi5 * xi2;
-    T f = ec * (T(0.75) * a * ir + T(0.5) * a3 * ir3) +
-          e * rsp * (T(4) * xi7 * a3 * r2 * r2 + T(3) * xi3 * a * r2 - T(20) * xi5 * a3 * r2 -
-                     T(4.5) * xi * a + T(14) * xi3 * a3 + xi * a3 * ir2);
-    T g = ec * (T(0.75) * a * ir - T(1.5) * a3 * ir3) +
-          e * rsp * (-T(4) * xi7 * a3 * r2 * r2 - T(3) * xi3 * a * r2 + T(16) * xi5 * a3 * r2 +
-                     T(1.5) * xi * a - T(2) * xi3 * a3 - T(3) * xi * a3 * ir2);
-    if (r < T(2) * a) {
-        f += (T(1) - T(9) * r / (T(32) * a)) - (T(0.75) * a * ir + T(0.5) * a3 * ir3);
-        g += (T(3) * r / (T(32) * a)) - (T(0.75) * a * ir - T(1.5) * a3 * ir3);
-    }
+    const T f = ec * (T(0.75) * a * ir + T(0.5) * a3 * ir3) +
+                e * rsp * (T(4) * xi7 * a3 * r2 * r2 + T(3) * xi3 * a * r2 - T(20) * xi5 * a3 * r2 -
+                           T(4.5) * xi * a + T(14) * xi3 * a3 + xi * a3 * ir2);
+    const T g = ec * (T(0.75) * a * ir - T(1.5) * a3 * ir3) +
+                e * rsp * (-T(4) * xi7 * a3 * r2 * r2 - T(3) * xi3 * a * r2 + T(16) * xi5 * a3 * r2 +
+                           T(1.5) * xi * a - T(2) * xi3 * a3 - T(3) * xi * a3 * ir2);
     F = f / a;
     G = g / a;
 }
@@ -137,7 +181,8 @@ constexpr int kCap = 512;  // candidates staged in shared memory per cell
 //      vectors (all lanes busy);
 //   3. lanes as (pair, right-hand side) apply the batch to the forces:
 //      u_i[r] += F f_j[r] + G rhat (rhat . f_j[r]).
-// Sums over one batch run in T; batches are accumulated in FP64.  No block
+// Sums over one batch run in T; across batches FP64 engines add in FP64 and
+// FP32 engines in compensated FP32 (TwoSum, PairSum below).  No block
 // barrier after the staging.  More than kCap candidates (very dense cells)
 // take a second path that reads candidates straight from global memory.
 // FP32: 64 registers, 16 blocks (32 warps) per SM (measured faster than the
@@ -270,7 +315,8 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
                         Gv = (T)Gd;
                     }
                     if (!done) real_FG<T>((T)rr, xi, a, Fv, Gv);
-                    const G ir = G(1) / rr;
+                    // coincident particles (r = 0): no direction, the G term vanishes
+                    const G ir = rr > G(0) ? G(1) / rr : G(0);
                     PairRec &pq = prec[warp][lane];
                     pq.rf.x = (T)(d0 * ir);
                     pq.rf.y = (T)(d1 * ir);
@@ -395,22 +441,47 @@ cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, 
 
 namespace {
 
-// real_FG on the host (same formula, std::erfc / std::exp in FP64).
+// real_FG on the host (same formulas, std::erf / std::erfc / std::exp in FP64).
 void host_real_FG(double r, double xi, double a, double &F, double &G) {
+    static const double ser_s[10] = {1.0, -1.0 / 3, 1.0 / 10, -1.0 / 42, 1.0 / 216,
+                                     -1.0 / 1320, 1.0 / 9360, -1.0 / 75600,
+                                     1.0 / 685440, -1.0 / 6894720};
+    static const double ser_p[10] = {2.0 / 3, -2.0 / 5, 1.0 / 7, -1.0 / 27, 1.0 / 132,
+                                     -1.0 / 780, 1.0 / 5400, -1.0 / 42840,
+                                     1.0 / 383040, -1.0 / 3810240};
     const double rsp = 0.56418958354775628695;
-    const double xr = xi * r, e = std::exp(-xr * xr), ec = std::erfc(xr);
+    const double x = xi * r, x2 = x * x, e = std::exp(-x2);
+    if (r < 2.0 * a) {
+        double S = 0.0, P = 0.0;
+        if (x < 0.5) {
+            for (int k = 9; k >= 0; k--) {
+                S = S * x2 + ser_s[k];
+                P = P * x2 + ser_p[k];
+            }
+            S *= 2.0 * rsp;
+            P *= 2.0 * rsp;
+        } else {
+            const double ef = std::erf(x);
+            S = ef / x;
+            P = (ef - 2.0 * rsp * x * e) / (x2 * x);
+        }
+        const double x4 = x2 * x2, xi3a2 = xi * xi * xi * a * a;
+        F = xi * (-0.75 * S + rsp * e * (3.0 * x2 - 4.5)) +
+            xi3a2 * (-0.5 * P + rsp * e * (4.0 * x4 - 20.0 * x2 + 14.0)) +
+            (1.0 - 9.0 * r / (32.0 * a)) / a;
+        G = xi * (-0.75 * S + rsp * e * (1.5 - 3.0 * x2)) +
+            xi3a2 * (1.5 * P + rsp * e * (-4.0 * x4 + 16.0 * x2 - 2.0)) + 3.0 * r / (32.0 * a * a);
+        return;
+    }
+    const double ec = std::erfc(x);
     const double r2 = r * r, a3 = a * a * a, ir = 1.0 / r, ir3 = ir * ir * ir, ir2 = ir * ir;
     const double xi2 = xi * xi, xi3 = xi2 * xi, xi5 = xi3 * xi2, xi7 = xi5 * xi2;
-    double f = ec * (0.75 * a * ir + 0.5 * a3 * ir3) +
-               e * rsp * (4.0 * xi7 * a3 * r2 * r2 + 3.0 * xi3 * a * r2 - 20.0 * xi5 * a3 * r2 -
-                          4.5 * xi * a + 14.0 * xi3 * a3 + xi * a3 * ir2);
-    double g = ec * (0.75 * a * ir - 1.5 * a3 * ir3) +
-               e * rsp * (-4.0 * xi7 * a3 * r2 * r2 - 3.0 * xi3 * a * r2 + 16.0 * xi5 * a3 * r2 +
-                          1.5 * xi * a - 2.0 * xi3 * a3 - 3.0 * xi * a3 * ir2);
-    if (r < 2.0 * a) {
-        f += (1.0 - 9.0 * r / (32.0 * a)) - (0.75 * a * ir + 0.5 * a3 * ir3);
-        g += (3.0 * r / (32.0 * a)) - (0.75 * a * ir - 1.5 * a3 * ir3);
-    }
+    const double f = ec * (0.75 * a * ir + 0.5 * a3 * ir3) +
+                     e * rsp * (4.0 * xi7 * a3 * r2 * r2 + 3.0 * xi3 * a * r2 - 20.0 * xi5 * a3 * r2 -
+                                4.5 * xi * a + 14.0 * xi3 * a3 + xi * a3 * ir2);
+    const double g = ec * (0.75 * a * ir - 1.5 * a3 * ir3) +
+                     e * rsp * (-4.0 * xi7 * a3 * r2 * r2 - 3.0 * xi3 * a * r2 + 16.0 * xi5 * a3 * r2 +
+                                1.5 * xi * a - 2.0 * xi3 * a3 - 3.0 * xi * a3 * ir2);
     F = f / a;
     G = g / a;
 }

@@ -236,3 +236,68 @@ def test_fp64_real_space_pairs_across_the_table_ranges(gpu_lib, radius):
     # the pair part alone (self term removed) at the same tolerance
     self_c = oracle.self_coeff(xi, a)
     assert relerr(u - self_c * f, ref - self_c * f) < 1e-11
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
+def test_close_and_coincident_pairs(gpu_lib, precision, tol):
+    """Pairs far inside the overlap range (r down to 1e-4 a) and coincident
+    particles (r = 0, where the pair has no direction) among random ones: the
+    real-space functions for r < 2a are evaluated in a form whose 1/r and 1/r^3
+    terms cancel analytically, so FP32 stays within its tolerance and FP64
+    within 1e-12 of the oracle."""
+    rng = np.random.default_rng(23)
+    n0, L, K, p, xi, rc, R = 3000, 60.0, 64, 6, 0.3, 10.0, 3
+    pos = rng.uniform(0.0, L, size=(n0, 3))
+    seps = [0.0, 1e-4, 1e-3, 0.01, 0.05, 0.2, 0.5, 1.0, 1.9]
+    extra = []
+    for k, s_ in enumerate(seps):
+        d = rng.standard_normal(3)
+        d *= s_ / np.linalg.norm(d)
+        extra.append(pos[k] + d)
+    pos = np.mod(np.vstack([pos, np.array(extra)]), L)
+    n = pos.shape[0]
+    f = rng.standard_normal((R, 3 * n))
+    eng = spme_gb300.Engine(n, L, xi, K, p, rcut=rc, precision=precision, max_nrhs=R,
+                            terms=spme_gb300.TERM_ALL)
+    eng.set_positions(pos)
+    u = eng.apply(f.astype(eng.dtype))
+    eng.close()
+    ref = oracle.full(pos, L, xi, rc, K, p, f.astype(eng.dtype).astype(np.float64), nthreads=4)
+    assert np.all(np.isfinite(u))
+    err = relerr(u, ref)
+    assert err < tol, err
+    # the particles of the close pairs alone, at the same tolerance
+    rows = np.concatenate([np.arange(3 * k, 3 * k + 3) for k in
+                           list(range(len(seps))) + list(range(n0, n))])
+    assert relerr(u[:, rows], ref[:, rows]) < tol
+
+
+# (N, L, K, p, R): FP32 column-gather spread with 1, 2 and 3 components per lane
+# and two component chunks (R = 20: 60 components)
+FP32_SPREAD_CASES = [
+    (1500, 45.0, 48, 6, 3),
+    (1500, 45.0, 40, 4, 8),
+    (1200, 40.0, 36, 8, 11),
+    (2000, 60.0, 64, 6, 20),
+]
+
+
+@pytest.mark.parametrize("case", FP32_SPREAD_CASES)
+def test_fp32_column_gather_spread_vs_oracle(gpu_lib, case):
+    """The FP32 column-gather spread (plane pairs with the packed two-lane FMA,
+    offset-ranked visits, padded force rows) against the tile spread and the
+    FP64 oracle."""
+    n, L, K, p, R = case
+    xi = 0.35
+    pos, f = uniform_case(n, L, R, seed=3 * K + R)
+    out = {}
+    for mode in (0, 1):
+        eng = spme_gb300.Engine(n, L, xi, K, p, precision="fp32", max_nrhs=R,
+                                terms=spme_gb300.TERM_RECIP)
+        eng.set_spread_mode(mode)
+        eng.set_positions(pos)
+        out[mode] = eng.apply(f.astype(np.float32))
+        eng.close()
+    ref = oracle.recip(pos, L, xi, K, p, f.astype(np.float32).astype(np.float64), nthreads=4)
+    assert relerr(out[1], out[0]) < 2e-6
+    assert relerr(out[1], ref) < FP32_TOL
