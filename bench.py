@@ -47,7 +47,7 @@ WORKLOADS = {
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) measured with
 # ncu at full size on the large workload, FP32, R = 16, tile 16x8x4 (a 1-pass metric
-# set); the command is in profiles/dram_large_fp32_r16.md.
+# set).
 NCU_TRAFFIC = {
     "large": {"spread": 816276224 + 3165029120, "influence": 3314295808 + 3188499968,
               "interp": 9328435968 + 200112640},
@@ -145,63 +145,152 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_oracle_time(w, reps_min=1, budget_s=20.0):
-    """The oracle (C restatement of the reference path + Beenakker real/self),
-    FP64, all host cores, one right-hand side of the full system per rep."""
+def _ref_lib_available():
     import oracle
-    oracle.build()
+    oracle.build(reference=True)
+    return os.path.exists(oracle.REF_COLORED_SO)
+
+
+def _real_self_time(w, pos, f1, nth, reps):
+    """The real-space + self part (absent from the reference): the oracle's
+    FP64 restatement of Beenakker's sum, best of `reps`."""
+    import oracle
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.real_self(pos, w["L"], w["xi"], w["rc"], f1, radius=w["a"], nthreads=nth)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best
+
+
+def _reference_recip_time(w, pos, f1, nth, reps, colored=True):
+    """The reference's own compute_spme (old-version/spme.c:560-726) on `nth`
+    OpenMP threads, one right-hand side of the full system with new positions
+    (its P build included), best of `reps`; returns (seconds, its phase timers)."""
+    import oracle
+    ref = oracle.Reference(w["xi"], w["K"], w["p"], w["N"], w["L"], nthreads=nth,
+                           colored=colored)
+    best, phases = None, {}
+    try:
+        for _ in range(reps):
+            v = np.zeros((1, 3 * w["N"]))
+            t0 = time.perf_counter()
+            _, ph = ref.compute_with_timers(pos, 1, 1.0, f1, 3 * w["N"], 0.0, v, 3 * w["N"])
+            dt = time.perf_counter() - t0
+            if best is None or dt < best:
+                best, phases = dt, ph
+    finally:
+        ref.close()
+    return best, phases
+
+
+def cpu_baseline_time(w, nth=None, single_thread=True):
+    """CPU baseline of the full operator on the host cores, one right-hand side of
+    the whole system per rep (a step's work at R = 1):
+    * reciprocal part: the reference's own compute_spme, compiled unmodified from
+      its sources (coloured OpenMP spread), all cores, best of 2; the FFT phases
+      (the project's DFTI shim standing in for MKL) reported separately from the
+      reference's own timers; once more on 1 thread;
+    * real-space + self part: the oracle's restatement (the reference has none).
+    Where the reference build is absent, the oracle's restatement of the
+    reciprocal path stands in (kind "port")."""
+    import oracle
+    oracle.build(reference=True)
     pos, f = synth(w, seed=99)
     f1 = f[:1].astype(np.float64)
-    nth = os.cpu_count() or 1
-    times = []
-    t_start = time.perf_counter()
-    while len(times) < reps_min or (time.perf_counter() - t_start < budget_s and len(times) < 3):
-        t0 = time.perf_counter()
-        oracle.full(pos, w["L"], w["xi"], w["rc"], w["K"], w["p"], f1, radius=w["a"],
-                    nthreads=nth)
-        times.append(time.perf_counter() - t0)
-    t = min(times)
-    t0 = time.perf_counter()
-    oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f1, radius=w["a"], nthreads=nth)
-    t_recip = time.perf_counter() - t0
-    ns = t * 1e9 / w["N"]
-    return {"value": ns, "unit": UNIT, "cores": nth, "kind": "port",
-            "sample": f"1 right-hand side of the full N={w['N']} system per rep, best of "
-                      f"{len(times)}; FP64 oracle (reference recip path restated + real-space/self)",
-            "recip_only_value": t_recip * 1e9 / w["N"]}
+    nth = nth or (os.cpu_count() or 1)
+    N = w["N"]
+    t_rs = _real_self_time(w, pos, f1, nth, 2)
+    out = {"unit": UNIT, "cores": nth}
+    if _ref_lib_available():
+        t_rec, ph = _reference_recip_time(w, pos, f1, nth, 2)
+        out.update({
+            "kind": "reference",
+            "value": (t_rec + t_rs) * 1e9 / N,
+            "sample": f"1 right-hand side of the full N={N} system per rep, best of 2: the "
+                      "reference's compute_spme compiled unmodified (coloured OpenMP spread, "
+                      "project DFTI shim for MKL) + the oracle's real-space/self sum (absent "
+                      "from the reference)",
+            "reference_recip_ns": t_rec * 1e9 / N,
+            "port_real_self_ns": t_rs * 1e9 / N,
+            "reference_phases_s": ph,
+            "fft_phase_ns": (ph.get("forward_fft", 0.0) + ph.get("backward_fft", 0.0)) * 1e9 / N,
+        })
+        if single_thread:
+            # the reference's reciprocal path alone on 1 thread (one rep, ~10-20 s at
+            # N = 1e6); the real-space restatement is not the reference's code
+            t1, ph1 = _reference_recip_time(w, pos, f1, 1, 1)
+            out["single_thread"] = {
+                "cores": 1, "reference_recip_ns": t1 * 1e9 / N, "reference_phases_s": ph1,
+                "fft_phase_ns": (ph1.get("forward_fft", 0.0) + ph1.get("backward_fft", 0.0))
+                * 1e9 / N}
+    else:
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f1, radius=w["a"], nthreads=nth)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out.update({"kind": "port", "value": (best + t_rs) * 1e9 / N,
+                    "sample": f"1 right-hand side of the full N={N} system per rep, best of 2; "
+                              "the oracle's FP64 restatement of the reference path + real-space/"
+                              "self (reference build absent)",
+                    "port_recip_ns": best * 1e9 / N, "port_real_self_ns": t_rs * 1e9 / N})
+    return out
 
 
 def run_reference(args, w):
+    """The reference's CPU path on the host cores for the same workload: per step
+    one right-hand side of the full system with new positions (the reference's
+    compute_spme, plus the oracle's real-space/self sum it lacks)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    base = cpu_oracle_time(w, reps_min=1, budget_s=0.0)  # warm the build and caches
-    times = []
     import oracle
+    have_ref = _ref_lib_available()
     pos, f = synth(w, seed=7)
     f1 = f[:1].astype(np.float64)
     nth = os.cpu_count() or 1
+    N = w["N"]
+    ref = (oracle.Reference(w["xi"], w["K"], w["p"], N, w["L"], nthreads=nth, colored=True)
+           if have_ref else None)
+    times, phases = [], {}
     for k in range(args.warmup + args.steps):
+        v = np.zeros((1, 3 * N))
         t0 = time.perf_counter()
-        oracle.full(pos, w["L"], w["xi"], w["rc"], w["K"], w["p"], f1, radius=w["a"],
-                    nthreads=nth)
+        if ref is not None:
+            _, ph = ref.compute_with_timers(pos, 1, 1.0, f1, 3 * N, 0.0, v, 3 * N)
+        else:
+            ph = {}
+            oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f1, radius=w["a"], nthreads=nth)
+        oracle.real_self(pos, w["L"], w["xi"], w["rc"], f1, radius=w["a"], nthreads=nth)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(dt)
+            for key, val in ph.items():
+                phases[key] = phases.get(key, 0.0) + val / args.steps
+    if ref is not None:
+        ref.close()
     ms = 1e3 * statistics.mean(times)
-    value = ms * 1e6 / w["N"]
+    value = ms * 1e6 / N
+    kind = "reference" if have_ref else "port"
+    sample = ("each step: 1 right-hand side of the full system with new positions: the "
+              "reference's compute_spme compiled unmodified (coloured OpenMP spread, project "
+              "DFTI shim for MKL) + the oracle's real-space/self sum (absent from the reference)"
+              if have_ref else
+              "each step: 1 right-hand side of the full system, the oracle's FP64 restatement "
+              "of the reference path + real-space/self (reference build absent)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: positions U[0,L), forces N(0,1), seeded",
         "config": config_of(w, args),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                         "sample": "each step: 1 right-hand side of the full system, FP64 "
-                                   "oracle restatement of the reference CPU path "
-                                   "(compiled reference unavailable on this host)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "recip_only_ns": base["recip_only_value"],
+        "reference_phases_s_per_step": phases,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -230,10 +319,21 @@ def run_gb300(args, w):
 
     cpu_base = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu_base = cpu_oracle_time(w)  # before any GPU work in this process
+        cpu_base = cpu_baseline_time(w)  # before any GPU work in this process
 
     N, R = w["N"], w["R"]
     pos, f = synth(w, seed=1000 + rank)
+    # FP64 oracle of the first two right-hand sides of the timed inputs (before
+    # any GPU work): reciprocal and real-space + self parts kept apart
+    oref = None
+    if rank == 0 and not args.no_fp64 and not args.no_oracle_check:
+        import oracle
+        nth = os.cpu_count() or 1
+        f2 = f[:2].astype(np.float64)
+        o_rec = oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f2, radius=w["a"],
+                             nthreads=nth)
+        o_rs = oracle.real_self(pos, w["L"], w["xi"], w["rc"], f2, radius=w["a"], nthreads=nth)
+        oref = {"full": o_rec + o_rs, "real_self": o_rs}
     # a dedicated (non-default) stream: the engine launches on it and the CUDA
     # events below are recorded on it
     stream = torch.cuda.Stream()
@@ -343,12 +443,31 @@ def run_gb300(args, w):
         rel = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
         ns64 = ms64 * 1e6 / N
         kmax = np.pi * w["K"] / w["L"]
+        acc = {"rel_l2_fp32_vs_fp64": rel,
+               "spme_truncation_recip": float(np.exp(-kmax ** 2 / (4 * w["xi"] ** 2))),
+               "spme_truncation_real": float(np.exp(-(w["xi"] * w["rc"]) ** 2))}
+        if oref is not None:
+            def rel_np(a, b):
+                return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            acc["rel_l2_fp32_vs_oracle"] = rel_np(u_d[:2].double().cpu().numpy(), oref["full"])
+            acc["rel_l2_fp64_vs_oracle"] = rel_np(u64[:1].cpu().numpy(), oref["full"][:1])
+            # the FP32 real-space + self part alone
+            ers = spme_gb300.Engine(N, w["L"], w["xi"], w["K"], w["p"], radius=w["a"],
+                                    rcut=w["rc"], precision="fp32", max_nrhs=2,
+                                    terms=spme_gb300.TERM_REAL | spme_gb300.TERM_SELF)
+            ers.set_stream(stream.cuda_stream)
+            ers.set_positions(p64)
+            urs = torch.zeros((2, 3 * N), dtype=torch.float32, device="cuda")
+            ers.apply(f_d[:2].contiguous(), urs)
+            torch.cuda.synchronize()
+            acc["rel_l2_fp32_real_self_vs_oracle"] = rel_np(urs.double().cpu().numpy(),
+                                                            oref["real_self"])
+            acc["oracle_rhs_checked"] = 2
+            ers.close()
         extra = {"fp64_plain": {"value": ns64, "unit": UNIT, "ms_per_apply": ms64,
                                 "terms": "recip+real+self", "nrhs": 1},
                  "fp32_batched_speedup_vs_fp64_plain": ns64 / value,
-                 "accuracy": {"rel_l2_fp32_vs_fp64": rel,
-                              "spme_truncation_recip": float(np.exp(-kmax ** 2 / (4 * w["xi"] ** 2))),
-                              "spme_truncation_real": float(np.exp(-(w["xi"] * w["rc"]) ** 2))}}
+                 "accuracy": acc}
         e64.close()
 
     if rank != 0:
@@ -476,6 +595,8 @@ def main():
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true",
+                    help="skip the FP64 oracle check of the timed result (outside the timed region)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tile", default=None,
                     help="fixed mesh tile 'tx,ty,tz' instead of autotuning (e.g. for profiling)")

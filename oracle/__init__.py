@@ -177,6 +177,46 @@ class Reference:
                               ldout)
         return vec_out
 
+    def compute_with_timers(self, pos, nrhs, alpha, vec_in, ldin, beta, vec_out, ldout):
+        """compute() with the reference's own phase timers (its stdout lines
+        "compute P", "srpead", "forward fft", "applying influence", "backward fft",
+        "interpolate", "totally takes", old-version/spme.c:168-323,651-724 and
+        old-version/spme_kernel.c:41-66,122-224,257-308) captured from file
+        descriptor 1 and returned as {phase: seconds} (phases repeat per
+        right-hand side and are summed)."""
+        import re
+        import sys
+        import tempfile
+        libc = ctypes.CDLL(None)
+        sys.stdout.flush()
+        libc.fflush(None)
+        saved = os.dup(1)
+        with tempfile.TemporaryFile(mode="w+b") as tmp:
+            os.dup2(tmp.fileno(), 1)
+            try:
+                self.compute(pos, nrhs, alpha, vec_in, ldin, beta, vec_out, ldout)
+                libc.fflush(None)
+            finally:
+                os.dup2(saved, 1)
+                os.close(saved)
+            tmp.seek(0)
+            text = tmp.read().decode(errors="replace")
+        phases, head = {}, None
+        for line in text.splitlines():
+            m = re.search(r"totally takes\s+([0-9.eE+-]+)", line)
+            if m:
+                phases["total"] = phases.get("total", 0.0) + float(m.group(1))
+                continue
+            m = re.search(r"takes\s+([0-9.eE+-]+)\s+secs", line)
+            if m and head:
+                phases[head] = phases.get(head, 0.0) + float(m.group(1))
+                head = None
+                continue
+            h = line.strip().rstrip(".").strip()
+            if h and not h.startswith("Computing"):
+                head = {"srpead": "spread"}.get(h, h).replace(" ", "_")
+        return vec_out, phases
+
     def close(self):
         if self.h:
             self.lib.destroy_spme_engine(self.h)
