@@ -487,7 +487,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_srec_idx, sizeof(int) * n));
         TRY(dalloc(&e->d_srec_start, sizeof(uint32_t) * n));
         TRY(dalloc(&e->d_srec_w, e->elem * record_width(e) * n));
-        TRY(dalloc(&e->d_Fs, e->elem * C * n));
+        TRY(dalloc(&e->d_Fs, e->elem * (size_t)spme::spread_cols_row_width((int)C) * n));
     }
     TRY(alloc_tiles(e));
     TRY(dalloc(&e->d_rec_idx, sizeof(int) * n));
@@ -803,11 +803,12 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         // column gather where it applies; measured on GB300 (K = 256, N = 1e6): in FP64
         // it wins at every C (8.0 vs 19.6 ms at C = 3), in FP32 from C = 9 on (the
         // tile kernel's per-component cost is lower at C = 3, 6)
-        // (the kernel stages force-row offsets s C as 32-bit integers)
+        // (the kernel stages force-row offsets as 32-bit integers)
         const bool use_cols = e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem) &&
-                              (e->elem == 8 || C >= 9) && (long long)n * C < (1LL << 31);
+                              (e->elem == 8 || C >= 9) &&
+                              (long long)n * spme::spread_cols_row_width(C) < (1LL << 31);
         if (use_cols) {
-            spme::launch_gather_rows<T>(F, e->d_srec_idx, n, C, (T *)e->d_Fs, s);
+            spme::launch_gather_cols_rows<T>(F, e->d_srec_idx, n, C, (T *)e->d_Fs, s);
             TRY_CUDA(spme::launch_spread_cols<T>(e->d_soff, e->d_srec_start,
                                                  (const T *)e->d_srec_w, (const T *)e->d_Fs, C,
                                                  e->g, (T *)e->d_mesh, s));

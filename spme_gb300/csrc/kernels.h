@@ -56,6 +56,12 @@ cudaError_t launch_spread(const int *tile_off, const int *rec_idx, const uint32_
 // start_off[(sy K + sx) K + sz] the offsets of that order (K^3 + 1 entries),
 // Fs the force rows in the same order.  Usable when spread_cols_ok(K, C, elem).
 bool spread_cols_ok(int K, int C, size_t elem);
+// Row width (elements) of the force rows the column-gather spread reads: each
+// lane's components contiguous and padded (C <= 16: C, unpadded).
+int spread_cols_row_width(int C);
+// Fs[s] = the row of F[idx[s]] (C components) in that padded layout.
+template <typename T>
+void launch_gather_cols_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStream_t s);
 template <typename T>
 cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, const T *rec_w,
                                const T *Fs, int C, const MeshGeom &g, T *mesh, cudaStream_t s);

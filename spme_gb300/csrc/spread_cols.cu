@@ -16,30 +16,75 @@
 //   * the warp walks the p (p + 1) start columns that reach its column pair and
 //     their z runs, so every particle it visits covers at least one of its two
 //     columns (a half whose column is missed multiplies by a zero weight);
-//   * the particle's z offset relative to the tile selects, through a
-//     warp-uniform jump, straight-line code with compile-time plane indices;
+//   * visits are staged 32 at a time (one lane per visit: record, weights of
+//     both columns, force-row offset) and ranked by their z offset relative to
+//     the tile (a 5-bit radix rank from ballots), so the accumulation walks the
+//     offsets in a compile-time sequence, each with straight-line code for its
+//     planes: no per-visit dispatch;
+//   * FP32 accumulators are pairs of planes, updated with the packed
+//     two-lane FMA (fma.rn.f32x2, sm_100 and later): a visit whose first plane
+//     is odd uses weights staged one plane later (0, w_0 .. w_{p-1}, 0);
+//   * force rows are read as one vector per lane: the rows are gathered per
+//     pass into a padded layout where each lane's CPL components are
+//     contiguous (spread_cols_row_width);
 //   * the block's columns are transposed through shared memory and written as
 //     whole mesh rows (coalesced), once: no zeroing, no atomics.
 // Mesh layout: component-major mesh[c][z][y][x] (the cuFFT batch layout).
+#include <utility>
+
 #include "kernels.h"
 
 namespace spme {
 
 namespace {
 
+// fn(std::integral_constant<int, i>) for i = 0 .. N-1, unrolled at compile time.
+template <typename Fn, int... Is>
+__device__ __forceinline__ void static_for_impl(Fn &&fn, std::integer_sequence<int, Is...>) {
+    (fn(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, typename Fn>
+__device__ __forceinline__ void static_for(Fn &&fn) {
+    static_for_impl(fn, std::make_integer_sequence<int, N>{});
+}
+
+// Asynchronous global -> shared copies (cp.async, completion tracked per thread).
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+}
+template <int B>
+__device__ __forceinline__ void cp_async_small(void *dst, const void *src) {
+    static_assert(B == 4 || B == 8, "4 or 8 bytes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src),
+                 "n"(B)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 template <typename T> struct V16;
 template <> struct V16<float> { using type = float4; };
 template <> struct V16<double> { using type = double2; };
 
-// p weights from a 16-byte aligned address, global or shared (vector loads
+// Components per lane for C components (chunks of 16 CPL components per block).
+__host__ __device__ constexpr int cols_cpl(int C) { return C <= 16 ? 1 : (C <= 32 ? 2 : 3); }
+// Padded components per lane in the gathered force rows.
+__host__ __device__ constexpr int cols_pcpl(int cpl) { return cpl == 3 ? 4 : cpl; }
+
+// n values from a 16-byte aligned address, global or shared (vector loads
 // where they fit).
-template <typename T, int P>
-__device__ __forceinline__ void load_weights(const T *__restrict__ src, T (&w)[P]) {
+template <typename T, int NV>
+__device__ __forceinline__ void load_vec(const T *__restrict__ src, T (&w)[NV]) {
     constexpr int VW = 16 / (int)sizeof(T);
-    constexpr int NV = P / VW;
+    constexpr int NQ = NV / VW;
     using V = typename V16<T>::type;
 #pragma unroll
-    for (int v = 0; v < NV; v++) {
+    for (int v = 0; v < NQ; v++) {
         const V q = reinterpret_cast<const V *>(src)[v];
         if constexpr (VW == 4) {
             w[4 * v] = q.x;
@@ -52,33 +97,67 @@ __device__ __forceinline__ void load_weights(const T *__restrict__ src, T (&w)[P
         }
     }
 #pragma unroll
-    for (int j = NV * VW; j < P; j++) w[j] = src[j];
+    for (int j = NQ * VW; j < NV; j++) w[j] = src[j];
 }
 
-// acc[D + j] += wt[j] f for the planes D + j inside [0, TZ) (wt[j] = w_x w_y w_z[j]).
-template <typename T, int P, int CPL, int TZ, int D>
-__device__ __forceinline__ void add_planes(T (&acc)[TZ][CPL], const T (&wt)[P],
-                                           const T (&f)[CPL]) {
+// Staged weight row length: FP32 rows hold p + 2 values (the first plane of an
+// odd offset shifted by one, so pairs of planes line up), FP64 rows p; both
+// padded to 16 bytes.
+template <typename T, int P>
+struct WRow {
+    static constexpr int raw = sizeof(T) == 4 ? P + 2 : P;
+    static constexpr int per16 = 16 / (int)sizeof(T);
+    static constexpr int value = (raw + per16 - 1) / per16 * per16;
+};
+
+// FP32: acc[m][k] holds planes (2m, 2m+1) of component k; a visit whose first
+// plane is D adds (w[2i], w[2i+1]) f_k to the pairs m = floor(D/2) + i that lie
+// inside [0, TZ/2) (w staged shifted by one plane for odd D).
+template <int P, int CPL, int TZ, int D, int NW>
+__device__ __forceinline__ void add_pairs(float2 (&acc)[TZ / 2][CPL], const float (&w)[NW],
+                                          const float (&f)[CPL]) {
+    constexpr int ODD = D & 1;
+    constexpr int M0 = (D - ODD) / 2;
+    constexpr int NPAIR = P / 2 + ODD;
+    float2 fd[CPL];
 #pragma unroll
-    for (int j = 0; j < P; j++) {
-        constexpr int lo = D < 0 ? -D : 0;
-        if (j >= lo && D + j < TZ) {
+    for (int k = 0; k < CPL; k++) fd[k] = make_float2(f[k], f[k]);
 #pragma unroll
-            for (int k = 0; k < CPL; k++) acc[D + j][k] += wt[j] * f[k];
+    for (int i = 0; i < NPAIR; i++) {
+        const int m = M0 + i;
+        if (m >= 0 && m < TZ / 2) {
+            const float2 wp = make_float2(w[2 * i], w[2 * i + 1]);
+#pragma unroll
+            for (int k = 0; k < CPL; k++) acc[m][k] = __ffma2_rn(wp, fd[k], acc[m][k]);
         }
     }
 }
 
+// FP64: acc[D + j][k] += w[j] f_k for the planes D + j inside [0, TZ).
+template <int P, int CPL, int TZ, int D, int NW>
+__device__ __forceinline__ void add_planes(double (&acc)[TZ][CPL], const double (&w)[NW],
+                                           const double (&f)[CPL]) {
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+        if (D + j >= 0 && D + j < TZ) {
+#pragma unroll
+            for (int k = 0; k < CPL; k++) acc[D + j][k] = fma(w[j], f[k], acc[D + j][k]);
+        }
+    }
+}
+
+template <typename T, int TZ, int CPL> struct AccType;
+template <int TZ, int CPL> struct AccType<float, TZ, CPL> { using type = float2[TZ / 2][CPL]; };
+template <int TZ, int CPL> struct AccType<double, TZ, CPL> { using type = double[TZ][CPL]; };
+
 // Per-warp shared scratch: the warp's start-column table (z runs and visit
-// prefix) and one batch of 32 staged particles.
+// prefix) and one batch of 32 staged visits in offset order.
 template <typename T, int P>
 struct WarpScratch {
     static constexpr int NQ = P * (P + 1);
-    static constexpr int PW = (P * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T);  // padded P
-    // staged visit: w_x w_y w_z[j] for the pair's two columns (16-byte rows), then
-    // (z offset, row of Fs)
-    __align__(16) T wt[32][2][PW];
-    int2 dz_row[32];  // (z offset, force-row offset s C)
+    static constexpr int WR = WRow<T, P>::value;
+    __align__(16) T wt[32][2][WR];  // weights of the pair's two columns
+    int row[32];                    // force-row offset (elements) of the visit
     int begA[NQ], nA[NQ], begB[NQ];
     int pre[NQ + 1];
 };
@@ -86,17 +165,26 @@ struct WarpScratch {
 template <typename T, int P, int CPL, int TZ, int NW>
 __global__ void __launch_bounds__(NW * 32, (sizeof(T) == 4 ? 3 : 1))
 k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_start,
-              const T *__restrict__ rec_w, const T *__restrict__ Fs, int C, int K, int nzt,
-              T *__restrict__ mesh) {
+              const T *__restrict__ rec_w, const T *__restrict__ Fs, int C, int RW, int K,
+              int nzt, T *__restrict__ mesh) {
+    constexpr bool F32 = sizeof(T) == 4;
     constexpr int WS = RecordWidth<T, P>::value;
+    constexpr int WR = WRow<T, P>::value;
+    constexpr int PC = cols_pcpl(CPL);  // padded components per lane in a force row
     constexpr int XT = 2 * NW;          // columns per block
     constexpr int CC = 16 * CPL;        // components per block
     constexpr int NX = P + 1;           // start columns per column pair (x)
     constexpr int NQ = P * NX;          // start columns per column pair (x and y)
+    constexpr int ND = TZ + P - 1;      // z offsets -(P-1) .. TZ-1
+    static_assert(ND <= 31 && TZ % 2 == 0, "offsets rank in 5 bits; plane pairs");
     // shared stride per component, padded so the two half-warps' column stores fall
     // on different banks (even / odd words in FP32)
-    constexpr int ROW = TZ * XT + (sizeof(T) == 4 ? 2 : 1);
-    static_assert(-(P - 1) >= -7 && TZ <= 16, "jump table covers offsets -7 .. 15");
+    constexpr int ROW = TZ * XT + (F32 ? 2 : 1);
+    // a staged force row (this block's chunk: 16 lanes x PC values) and the visits
+    // per batch: the batch's rows share the transpose buffer, NB rows per warp
+    constexpr int LR = 16 * PC;
+    constexpr int NB = (CC * ROW) / (NW * LR) < 32 ? (CC * ROW) / (NW * LR) : 32;
+    static_assert(NB >= 8, "staged batch");
     extern __shared__ __align__(16) unsigned char sp_raw[];
     T *tsm = reinterpret_cast<T *>(sp_raw);  // [CC][ROW] transpose buffer
     const size_t tsm_bytes = ((size_t)CC * ROW * sizeof(T) + 15) & ~(size_t)15;
@@ -112,16 +200,23 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
     const int xa = x0 + 2 * warp;  // first column of the warp's pair
     WarpScratch<T, P> &ws = reinterpret_cast<WarpScratch<T, P> *>(sp_raw + tsm_bytes)[warp];
 
-    T acc[TZ][CPL];
+    typename AccType<T, TZ, CPL>::type acc;
+    if constexpr (F32) {
 #pragma unroll
-    for (int z = 0; z < TZ; z++)
+        for (int m = 0; m < TZ / 2; m++)
 #pragma unroll
-        for (int k = 0; k < CPL; k++) acc[z][k] = T(0);
-    // this lane's components: Fs + row offset + 16 k, valid where c < C
-    const T *fbase = Fs + cb + l16;
-    bool cval[CPL];
+            for (int k = 0; k < CPL; k++) acc[m][k] = make_float2(0.f, 0.f);
+    } else {
 #pragma unroll
-    for (int k = 0; k < CPL; k++) cval[k] = cb + l16 + 16 * k < C;
+        for (int z = 0; z < TZ; z++)
+#pragma unroll
+            for (int k = 0; k < CPL; k++) acc[z][k] = 0.0;
+    }
+    // the warp's staged force rows of one batch (in the transpose buffer, free
+    // until the write-out); this lane's components of row j at j LR + l16 PC
+    // (CPL = 1: component l16, present when l16 < C)
+    T *fst = tsm + (size_t)warp * NB * LR;
+    const bool lane_live = CPL > 1 || l16 < C;
 
     if (xa < K) {
         // start-column table: z runs of start cells that reach [z0, z0 + ext),
@@ -160,9 +255,11 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
         __syncwarp();
         const int M = run;  // visits of this warp
 
-        for (int vb = 0; vb < M; vb += 32) {
-            const int nb = min(32, M - vb);
-            // stage: lane t fetches visit vb + t
+        for (int vb = 0; vb < M; vb += NB) {
+            const int nb = min(NB, M - vb);
+            // stage: lane t fetches visit vb + t; dl = its z offset + P - 1 (31: none)
+            int dl = 31, s = 0;
+            uint32_t st = 0;
             if (lane < nb) {
                 const int v = vb + lane;
                 int a = 0, b = NQ;  // pre[a] <= v < pre[b]
@@ -172,9 +269,30 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 }
                 const int r = v - ws.pre[a];
                 const bool partB = r >= ws.nA[a];
-                const int s = partB ? ws.begB[a] + (r - ws.nA[a]) : ws.begA[a] + r;
+                s = partB ? ws.begB[a] + (r - ws.nA[a]) : ws.begA[a] + r;
+                st = __ldg(rec_start + s);
+                // dz in [-(P-1), ext)
+                dl = (int)((st >> 20) & 1023u) - (partB ? z0 + K : z0) + (P - 1);
+            }
+            // rank by offset: lanes with a smaller offset, then equal offsets in lane order
+            unsigned eq = 0xffffffffu;
+            int lt = 0;
+#pragma unroll
+            for (int bit = 4; bit >= 0; bit--) {
+                const bool one = (dl >> bit) & 1;
+                const unsigned bm = __ballot_sync(0xffffffffu, one);
+                if (one) {
+                    lt += __popc(eq & ~bm);
+                    eq &= bm;
+                } else {
+                    eq &= ~bm;
+                }
+            }
+            const int pos = lt + __popc(eq & ((1u << lane) - 1u));
+            if (lane < nb) {
+                ws.row[pos] = s * RW;  // CPL = 1: RW = C
                 int sx, sy, sz;
-                unpack_start(__ldg(rec_start + s), sx, sy, sz);
+                unpack_start(st, sx, sy, sz);
                 int ox = xa - sx;
                 if (ox < 0) ox += K;
                 int oy = y - sy;
@@ -186,79 +304,98 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
                 const int ox1 = ox + 1 == K ? 0 : ox + 1;
                 const T w0 = ox < P ? wy * __ldg(rw + ox) : T(0);
                 const T w1 = (ox1 < P && xa + 1 < K) ? wy * __ldg(rw + ox1) : T(0);
-                // dz in [-(P-1), ext); the visit's force row as an offset (s C < 2^31)
-                ws.dz_row[lane] = make_int2(sz - (partB ? z0 + K : z0), s * C);
                 T wz[P];
-                load_weights<T, P>(rw + 2 * P, wz);
-                // 16-byte stores (scalar stores at this lane stride conflict 16-way)
-                constexpr int PW = WarpScratch<T, P>::PW, VW = 16 / (int)sizeof(T);
+                load_vec<T, P>(rw + 2 * P, wz);
+                // weight rows of both columns (16-byte stores; scalar stores at this
+                // lane stride conflict 16-way)
+                constexpr int VW = 16 / (int)sizeof(T);
                 using V = typename V16<T>::type;
+                const int shift = F32 ? ((dl - (P - 1)) & 1) : 0;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const T w = h ? w1 : w0;
-                    T row[PW];
+                    T row[WR];
 #pragma unroll
-                    for (int j = 0; j < PW; j++) row[j] = j < P ? w * wz[j] : T(0);
+                    for (int j = 0; j < WR; j++) {
+                        // j - shift in [0, P): weight of plane j - shift of the stencil
+                        const T a0 = (j < P) ? wz[j < P ? j : 0] : T(0);
+                        const T a1 = (j >= 1 && j - 1 < P) ? wz[j >= 1 && j - 1 < P ? j - 1 : 0] : T(0);
+                        row[j] = w * (shift ? a1 : a0);
+                    }
 #pragma unroll
-                    for (int v = 0; v < PW / VW; v++) {
-                        V q;
+                    for (int q = 0; q < WR / VW; q++) {
+                        V qv;
                         if constexpr (VW == 4) {
-                            q.x = row[4 * v];
-                            q.y = row[4 * v + 1];
-                            q.z = row[4 * v + 2];
-                            q.w = row[4 * v + 3];
+                            qv.x = row[4 * q];
+                            qv.y = row[4 * q + 1];
+                            qv.z = row[4 * q + 2];
+                            qv.w = row[4 * q + 3];
                         } else {
-                            q.x = row[2 * v];
-                            q.y = row[2 * v + 1];
+                            qv.x = row[2 * q];
+                            qv.y = row[2 * q + 1];
                         }
-                        reinterpret_cast<V *>(&ws.wt[lane][h][0])[v] = q;
+                        reinterpret_cast<V *>(&ws.wt[pos][h][0])[q] = qv;
                     }
                 }
             }
             __syncwarp();
-            // accumulate the batch (force row of the next visit prefetched)
-            T fn[CPL];
-            {
-                const T *row = fbase + ws.dz_row[0].y;
-#pragma unroll
-                for (int k = 0; k < CPL; k++) fn[k] = cval[k] ? __ldg(row + 16 * k) : T(0);
-            }
-            for (int j = 0; j < nb; j++) {
-                T f[CPL];
-#pragma unroll
-                for (int k = 0; k < CPL; k++) f[k] = fn[k];
-                const int2 dr = ws.dz_row[j];
-                if (j + 1 < nb) {
-                    const T *row = fbase + ws.dz_row[j + 1].y;
-#pragma unroll
-                    for (int k = 0; k < CPL; k++) fn[k] = cval[k] ? __ldg(row + 16 * k) : T(0);
+            // the batch's force rows, in offset order, into shared memory: one
+            // round trip per batch instead of one per visit
+            if constexpr (CPL > 1) {
+                constexpr int VW = 16 / (int)sizeof(T);
+                constexpr int NCH = LR / VW;  // 16-byte pieces per row
+                for (int t = lane; t < nb * NCH; t += 32) {
+                    const int v = t / NCH, q = t - v * NCH;
+                    cp_async16(fst + v * LR + q * VW, Fs + ws.row[v] + (size_t)chunk * LR + q * VW);
                 }
-                T wt[P];
-                load_weights<T, P>(&ws.wt[j][half][0], wt);
-                switch (dr.x) {
-#define SPME_SPC(DD)                                                                      \
-    case DD:                                                                              \
-        if constexpr (DD >= -(P - 1) && DD < TZ) add_planes<T, P, CPL, TZ, DD>(acc, wt, f); \
-        break;
-                    SPME_SPC(-7) SPME_SPC(-6) SPME_SPC(-5) SPME_SPC(-4) SPME_SPC(-3)
-                    SPME_SPC(-2) SPME_SPC(-1) SPME_SPC(0) SPME_SPC(1) SPME_SPC(2)
-                    SPME_SPC(3) SPME_SPC(4) SPME_SPC(5) SPME_SPC(6) SPME_SPC(7)
-                    SPME_SPC(8) SPME_SPC(9) SPME_SPC(10) SPME_SPC(11) SPME_SPC(12)
-                    SPME_SPC(13) SPME_SPC(14) SPME_SPC(15)
-#undef SPME_SPC
-                    default: break;
+            } else {
+                for (int t = lane; t < nb * 16; t += 32) {
+                    const int v = t >> 4, c = t & 15;
+                    if (c < C) cp_async_small<(int)sizeof(T)>(fst + v * LR + c, Fs + ws.row[v] + c);
                 }
             }
+            cp_async_wait_all();
+            __syncwarp();
+            // accumulate in offset order
+            int j = 0;
+            static_for<ND>([&](auto bc) {
+                constexpr int D = decltype(bc)::value - (P - 1);  // the bucket's z offset
+                const int cnt = __popc(__ballot_sync(0xffffffffu, dl == D + (P - 1)));
+                for (int k = 0; k < cnt; k++, j++) {
+                    T f[CPL];
+                    if constexpr (CPL > 1) {
+                        T fv[PC];
+                        load_vec<T, PC>(fst + j * LR + l16 * PC, fv);
+#pragma unroll
+                        for (int c = 0; c < CPL; c++) f[c] = fv[c];
+                    } else {
+                        f[0] = lane_live ? fst[j * LR + l16] : T(0);
+                    }
+                    T wt[WR];
+                    load_vec<T, WR>(&ws.wt[j][half][0], wt);
+                    if constexpr (F32)
+                        add_pairs<P, CPL, TZ, D, WR>(acc, wt, f);
+                    else
+                        add_planes<P, CPL, TZ, D, WR>(acc, wt, f);
+                }
+            });
             __syncwarp();
         }
     }
 
-    // transpose through shared memory: tsm[c][z][x]
+    // transpose through shared memory: tsm[c][z][x] (after every warp of the
+    // block is done with its staged force rows, which live in the same buffer)
+    __syncthreads();
     const int xl = 2 * warp + half;
 #pragma unroll
     for (int z = 0; z < TZ; z++)
 #pragma unroll
-        for (int k = 0; k < CPL; k++) tsm[(size_t)(l16 + 16 * k) * ROW + z * XT + xl] = acc[z][k];
+        for (int k = 0; k < CPL; k++) {
+            T v;
+            if constexpr (F32) v = (z & 1) ? acc[z >> 1][k].y : acc[z >> 1][k].x;
+            else v = acc[z][k];
+            tsm[(size_t)(l16 + 16 * k) * ROW + z * XT + xl] = v;
+        }
     __syncthreads();
     // whole rows of XT columns per (component, plane): each thread keeps one
     // (plane, column) slot and walks the components with pointer increments
@@ -277,6 +414,29 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
     }
 }
 
+// Fs[s][chunk*16*PC + l*PC + k] = F[idx[s]][chunk*16*CPL + l + 16 k] for k < CPL
+// (0 where that component does not exist or k >= CPL); CPL = 1: Fs[s][c] = F[idx[s]][c].
+template <typename T, int CPL>
+__global__ void k_gather_cols_rows(const T *__restrict__ F, const int *__restrict__ idx, int n,
+                                   int C, int RW, T *__restrict__ Fs) {
+    constexpr int PC = cols_pcpl(CPL);
+    const size_t total = (size_t)n * RW;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = t / RW;
+        const int q = (int)(t - s * RW);
+        int c;
+        if (CPL == 1) {
+            c = q;
+        } else {
+            const int chunk = q / (16 * PC), r = q - chunk * 16 * PC;
+            const int l = r / PC, k = r - l * PC;
+            c = k < CPL ? chunk * 16 * CPL + l + 16 * k : C;
+        }
+        Fs[t] = c < C ? F[(size_t)idx[s] * C + c] : T(0);
+    }
+}
+
 template <typename T, int P, int CPL>
 cudaError_t launch_cols(const int *soff, const uint32_t *rec_start, const T *rec_w, const T *Fs,
                         int C, const MeshGeom &g, T *mesh, cudaStream_t s) {
@@ -292,7 +452,8 @@ cudaError_t launch_cols(const int *soff, const uint32_t *rec_start, const T *rec
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((K + XT - 1) / XT, K, nzt * nchunk);
-    kern<<<grid, NW * 32, smem, s>>>(soff, rec_start, rec_w, Fs, C, K, nzt, mesh);
+    kern<<<grid, NW * 32, smem, s>>>(soff, rec_start, rec_w, Fs, C, spread_cols_row_width(C), K,
+                                     nzt, mesh);
     return cudaGetLastError();
 }
 
@@ -300,9 +461,16 @@ template <typename T, int P>
 cudaError_t dispatch_cpl(const int *soff, const uint32_t *rec_start, const T *rec_w, const T *Fs,
                          int C, const MeshGeom &g, T *mesh, cudaStream_t s) {
     // components per lane: the smallest CPL with 16 CPL >= C, at most 3
-    if (C <= 16) return launch_cols<T, P, 1>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
-    if (C <= 32) return launch_cols<T, P, 2>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
-    return launch_cols<T, P, 3>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
+    switch (cols_cpl(C)) {
+        case 1: return launch_cols<T, P, 1>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
+        case 2: return launch_cols<T, P, 2>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
+        default: return launch_cols<T, P, 3>(soff, rec_start, rec_w, Fs, C, g, mesh, s);
+    }
+}
+
+int blocks_for_rows(size_t total) {
+    const size_t b = (total + 255) / 256;
+    return (int)(b < 8192 ? (b > 0 ? b : 1) : 8192);
 }
 
 }  // namespace
@@ -314,6 +482,31 @@ cudaError_t dispatch_cpl(const int *soff, const uint32_t *rec_start, const T *re
 bool spread_cols_ok(int K, int C, size_t elem) {
     (void)elem;
     return K >= 32 && K <= 1024 && C >= 1;
+}
+
+int spread_cols_row_width(int C) {
+    const int cpl = cols_cpl(C);
+    if (cpl == 1) return C;
+    const int nchunk = (C + 16 * cpl - 1) / (16 * cpl);
+    return nchunk * 16 * cols_pcpl(cpl);
+}
+
+template <typename T>
+void launch_gather_cols_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStream_t s) {
+    const int RW = spread_cols_row_width(C);
+    const size_t total = (size_t)n * RW;
+    if (!total) return;
+    switch (cols_cpl(C)) {
+        case 1:
+            k_gather_cols_rows<T, 1><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW, Fs);
+            break;
+        case 2:
+            k_gather_cols_rows<T, 2><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW, Fs);
+            break;
+        default:
+            k_gather_cols_rows<T, 3><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW, Fs);
+            break;
+    }
 }
 
 template <typename T>
@@ -328,6 +521,10 @@ cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, 
     }
 }
 
+template void launch_gather_cols_rows<float>(const float *, const int *, int, int, float *,
+                                             cudaStream_t);
+template void launch_gather_cols_rows<double>(const double *, const int *, int, int, double *,
+                                              cudaStream_t);
 template cudaError_t launch_spread_cols<float>(const int *, const uint32_t *, const float *,
                                                const float *, int, const MeshGeom &, float *,
                                                cudaStream_t);
