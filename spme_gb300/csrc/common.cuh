@@ -117,6 +117,17 @@ struct DivMod {
     }
 };
 
+// The system of work item w in a batched launch: prefix[k] <= w < prefix[k + 1]
+// (prefix has nsys + 1 entries).
+__device__ __forceinline__ int batch_find(const int *__restrict__ prefix, int nsys, int w) {
+    int a = 0, b = nsys;
+    while (b - a > 1) {
+        const int m = (a + b) >> 1;
+        if (__ldg(prefix + m) <= w) a = m; else b = m;
+    }
+    return a;
+}
+
 template <typename T> struct Vec2;
 template <> struct Vec2<float> { using type = float2; };
 template <> struct Vec2<double> { using type = double2; };

@@ -21,6 +21,45 @@
 
 using spme::MeshGeom;
 
+namespace spme {
+
+// Host B-spline values M_p(w + p - 1 - j) (same recursion as the kernels).
+void host_bspline(int p, double w, double *out) {
+    double a[spme::kMaxP + 1];
+    a[0] = w;
+    a[1] = 1.0 - w;
+    for (int n = 3; n <= p; n++) {
+        a[n - 1] = 0.0;
+        for (int k = n - 1; k >= 1; k--)
+            a[k] = ((w + k) * a[k] + ((double)n - w - k) * a[k - 1]) / (double)(n - 1);
+        a[0] = w * a[0] / (double)(n - 1);
+    }
+    for (int k = 0; k < p; k++) out[k] = a[p - 1 - k];
+}
+
+// |b(m)|^2 = 1/|sum_{j<p-1} M_p(j+1) e^{i j phi}|^2, phi = 2 pi m'/K
+// (old-version/spme.c:109-126; only the modulus enters the table).
+void host_moduli2(int K, int p, std::vector<double> &out) {
+    double mp[spme::kMaxP];
+    host_bspline(p, 0.0, mp);  // mp[j] = M_p(p - 1 - j)
+    out.resize(K);
+    for (int m = 0; m < K; m++) {
+        int mm = m <= K / 2 ? m : m - K;
+        double phi = 2.0 * M_PI * (double)mm / (double)K;
+        double re = 0.0, im = 0.0;
+        for (int j = 0; j < p - 1; j++) {
+            double s = mp[p - 2 - j];
+            re += s * std::cos(j * phi);
+            im += s * std::sin(j * phi);
+        }
+        out[m] = 1.0 / (re * re + im * im);
+    }
+}
+
+}  // namespace spme
+
+using spme::host_moduli2;
+
 namespace {
 
 constexpr int kStages = 8;
@@ -185,39 +224,6 @@ int dalloc(P **p, size_t bytes) {
 
 void dfree(void *p) {
     if (p) cudaFree(p);
-}
-
-// Host B-spline values M_p(w + p - 1 - j) (same recursion as the kernels).
-void host_bspline(int p, double w, double *out) {
-    double a[spme::kMaxP + 1];
-    a[0] = w;
-    a[1] = 1.0 - w;
-    for (int n = 3; n <= p; n++) {
-        a[n - 1] = 0.0;
-        for (int k = n - 1; k >= 1; k--)
-            a[k] = ((w + k) * a[k] + ((double)n - w - k) * a[k - 1]) / (double)(n - 1);
-        a[0] = w * a[0] / (double)(n - 1);
-    }
-    for (int k = 0; k < p; k++) out[k] = a[p - 1 - k];
-}
-
-// |b(m)|^2 = 1/|sum_{j<p-1} M_p(j+1) e^{i j phi}|^2, phi = 2 pi m'/K
-// (old-version/spme.c:109-126; only the modulus enters the table).
-void host_moduli2(int K, int p, std::vector<double> &out) {
-    double mp[spme::kMaxP];
-    host_bspline(p, 0.0, mp);  // mp[j] = M_p(p - 1 - j)
-    out.resize(K);
-    for (int m = 0; m < K; m++) {
-        int mm = m <= K / 2 ? m : m - K;
-        double phi = 2.0 * M_PI * (double)mm / (double)K;
-        double re = 0.0, im = 0.0;
-        for (int j = 0; j < p - 1; j++) {
-            double s = mp[p - 2 - j];
-            re += s * std::cos(j * phi);
-            im += s * std::sin(j * phi);
-        }
-        out[m] = 1.0 / (re * re + im * im);
-    }
 }
 
 bool is_fp32(const spme_t *e) { return e->prm.precision == SPME_FP32; }
@@ -476,7 +482,7 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_pstart, sizeof(uint32_t) * n));
         TRY(dalloc(&e->d_pfrac, e->elem * 3 * n));
     }
-    e->cols = (prm.terms & SPME_TERM_RECIP) && spme::spread_cols_ok((int)K, (int)C, e->elem);
+    e->cols = (prm.terms & SPME_TERM_RECIP) && spme::spread_cols_ok((int)K, (int)C, e->elem, prm.porder);
     if (e->cols) {
         const size_t K3 = K * K * K;
         TRY(dalloc(&e->d_scount, sizeof(int) * K3));
@@ -804,7 +810,8 @@ int run_pass(spme_t *e, int R, const T *f, long ldf, T *u, long ldu, double alph
         // it wins at every C (8.0 vs 19.6 ms at C = 3), in FP32 from C = 9 on (the
         // tile kernel's per-component cost is lower at C = 3, 6)
         // (the kernel stages force-row offsets as 32-bit integers)
-        const bool use_cols = e->cols && e->spread_mode == 1 && spme::spread_cols_ok(K, C, e->elem) &&
+        const bool use_cols = e->cols && e->spread_mode == 1 &&
+                              spme::spread_cols_ok(K, C, e->elem, e->g.p) &&
                               (e->elem == 8 || C >= 9) &&
                               (long long)n * spme::spread_cols_row_width(C) < (1LL << 31);
         if (use_cols) {

@@ -15,6 +15,8 @@
 // pairs, the x offsets summed with shuffles.  Every particle is handled by
 // exactly one CTA; mesh values come from HBM about once and from L2 for the
 // halos.
+#include <algorithm>
+
 #include "kernels.h"
 #include "tma.cuh"
 
@@ -29,24 +31,30 @@ template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
 
+// One tile's work (the body of the single-system kernel and of the batched
+// one); tmap is read only when use_tma is set.
 template <typename T, int P, int CG>
-__global__ void __launch_bounds__(kThreads)
-k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
-         const int *__restrict__ tile_off, const int *__restrict__ rec_idx,
-         const uint32_t *__restrict__ rec_start, const T *__restrict__ rec_w,
-         const T *__restrict__ mesh, int C, int cb, int ce, MeshGeom g, T *__restrict__ W,
-         int accumulate, int *__restrict__ err) {
+__device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const InterpArgs<T> &A,
+                                            int tile) {
     using V = typename Vec16<T>::type;
     constexpr int VW = Vec16<T>::n;
     constexpr int NV = kHX / VW;  // vectors per staged row
-    constexpr int WS = RecordWidth<T, P>::value;
     constexpr int NG = CG / 4;    // groups of 4 components per chunk
+    const int use_tma = A.use_tma;
+    const int *__restrict__ tile_off = A.tile_off;
+    const int *__restrict__ rec_idx = A.rec_idx;
+    const uint32_t *__restrict__ rec_start = A.rec_start;
+    const T *__restrict__ rec_w = A.rec_w;
+    const T *__restrict__ mesh = A.mesh;
+    T *__restrict__ W = A.W;
+    int *__restrict__ err = A.err;
+    const MeshGeom &g = A.g;
+    const int C = A.C, cb = A.cb, ce = A.ce, accumulate = A.accumulate, WS = A.ws;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     // TMA destinations must be 128-byte aligned (128 spare bytes are allocated)
     T *box = reinterpret_cast<T *>(smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127));
 
-    const int tile = blockIdx.x;
     const int pbeg = tile_off[tile], pend = tile_off[tile + 1];
     if (pbeg == pend) return;
     const int K = g.K;
@@ -113,7 +121,7 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
             if (threadIdx.x == 0) {
                 fence_proxy_async();  // order earlier generic reads of the box before the TMA write
                 mbar_expect_tx(&bar, (uint32_t)((size_t)CG * PS * sizeof(T)));
-                tma_load_4d(box, &tmap, ox, oy, oz, c0, &bar);
+                tma_load_4d(box, tmap, ox, oy, oz, c0, &bar);
             }
             const bool ok = mbar_wait(&bar, (uint32_t)(chunk & 1));
             if (!__syncthreads_and(ok)) {  // uniform decision: all threads give up together
@@ -191,6 +199,31 @@ k_interp(const __grid_constant__ CUtensorMap tmap, int use_tma,
 }
 
 template <typename T, int P, int CG>
+__global__ void __launch_bounds__(kThreads)
+k_interp(const __grid_constant__ CUtensorMap tmap, InterpArgs<T> A) {
+    interp_body<T, P, CG>(&tmap, A, blockIdx.x);
+}
+
+// Many systems in one persistent launch over their tiles (plain-load staging,
+// no TMA); the order p of each system selects the body.
+template <typename T, int CG>
+__global__ void __launch_bounds__(kThreads)
+k_interp_batch(const InterpSys<T> *__restrict__ sys, const int *__restrict__ prefix, int nsys,
+               int total) {
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int k = batch_find(prefix, nsys, w);
+        const InterpSys<T> S = sys[k];
+        const int tile = w - prefix[k];
+        switch (S.args.g.p) {
+            case 4: interp_body<T, 4, CG>(nullptr, S.args, tile); break;
+            case 6: interp_body<T, 6, CG>(nullptr, S.args, tile); break;
+            default: interp_body<T, 8, CG>(nullptr, S.args, tile); break;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int P, int CG>
 size_t interp_smem(const MeshGeom &g) {
     return (size_t)CG * (g.tz + P - 1) * (g.ty + P - 1) * kHX * sizeof(T) + 128;
 }
@@ -207,9 +240,9 @@ cudaError_t launch_interp_t(const InterpMaps &maps, const int *tile_off, const i
     if (e != cudaSuccess) return e;
     const bool use = maps.ok4;
     const CUtensorMap &m = maps.cg4;
-    kern<<<g.ntx * g.nty * g.ntz, kThreads, smem, s>>>(m, use ? 1 : 0, tile_off, rec_idx,
-                                                      rec_start, rec_w, mesh, C, cb, ce, g, W,
-                                                      accumulate, err);
+    InterpArgs<T> A{tile_off, rec_idx, rec_start, rec_w, mesh, W, err, g, C, cb, ce,
+                    accumulate, use ? 1 : 0, RecordWidth<T, P>::value};
+    kern<<<g.ntx * g.nty * g.ntz, kThreads, smem, s>>>(m, A);
     return cudaGetLastError();
 }
 
@@ -267,6 +300,27 @@ cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, co
     }
 }
 
+template <typename T>
+cudaError_t launch_interp_batch(const InterpSys<T> *sys, const int *prefix, int nsys, int total,
+                                size_t smem, cudaStream_t s) {
+    if (total <= 0) return cudaSuccess;
+    auto kern = k_interp_batch<T, 4>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    const int grid = std::max(1, std::min(total, sms * std::max(per_sm, 1)));
+    kern<<<grid, kThreads, smem, s>>>(sys, prefix, nsys, total);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_interp_batch<float>(const InterpSys<float> *, const int *, int, int,
+                                                size_t, cudaStream_t);
+template cudaError_t launch_interp_batch<double>(const InterpSys<double> *, const int *, int, int,
+                                                 size_t, cudaStream_t);
 template cudaError_t launch_interp<float>(const InterpMaps &, const int *, int, const int *,
                                           const uint32_t *, const float *, const float *, int,
                                           int, int, const MeshGeom &, float *, int, int *,

@@ -54,14 +54,39 @@ cudaError_t launch_spread(const int *tile_off, const int *rec_idx, const uint32_
                           cudaStream_t s);
 // Column-gather spread (spread_cols.cu): records sorted by stencil-start cell,
 // start_off[(sy K + sx) K + sz] the offsets of that order (K^3 + 1 entries),
-// Fs the force rows in the same order.  Usable when spread_cols_ok(K, C, elem).
-bool spread_cols_ok(int K, int C, size_t elem);
+// Fs the force rows in the same order.  Usable when spread_cols_ok(K, C, elem, p).
+bool spread_cols_ok(int K, int C, size_t elem, int p);
 // Row width (elements) of the force rows the column-gather spread reads: each
 // lane's components contiguous and padded (C <= 16: C, unpadded).
 int spread_cols_row_width(int C);
 // Fs[s] = the row of F[idx[s]] (C components) in that padded layout.
 template <typename T>
 void launch_gather_cols_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStream_t s);
+// Arguments of one system's column-gather spread: start-cell offsets of this
+// system (indexed by its own (sy K + sx) K + sz), records and force rows
+// indexed by sorted slot, ws the record stride (elements).
+template <typename T>
+struct SpreadColsArgs {
+    const int *soff;
+    const uint32_t *rec_start;
+    const T *rec_w;
+    const T *Fs;
+    T *mesh;
+    int C, RW, K, nzt, ws;
+};
+// A system of a batched launch: its arguments, order and blocks along x.
+template <typename T>
+struct SpreadColsSys {
+    SpreadColsArgs<T> args;
+    int p, gx;
+};
+// Blocks of one system's column-gather spread (all component chunks).
+int spread_cols_blocks(int K, int C, size_t elem);
+// All systems (same C) in one persistent launch; prefix[k] = the first block
+// of system k (nsys + 1 entries, prefix[nsys] = total), both on the device.
+template <typename T>
+cudaError_t launch_spread_cols_batch(const SpreadColsSys<T> *sys, const int *prefix, int nsys,
+                                     int total, int C, cudaStream_t s);
 template <typename T>
 cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, const T *rec_w,
                                const T *Fs, int C, const MeshGeom &g, T *mesh, cudaStream_t s);
@@ -74,6 +99,29 @@ struct InterpMaps {
 bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem);
 // Shared memory the interpolation kernel needs (4-component boxes).
 size_t interp_smem_bytes(const MeshGeom &g, size_t elem);
+// Arguments of one system's interpolation (records indexed by sorted slot,
+// stride ws; tile_off indexed by this system's tiles; W rows by particle).
+template <typename T>
+struct InterpArgs {
+    const int *tile_off;
+    const int *rec_idx;
+    const uint32_t *rec_start;
+    const T *rec_w;
+    const T *mesh;
+    T *W;
+    int *err;
+    MeshGeom g;
+    int C, cb, ce, accumulate, use_tma, ws;
+};
+template <typename T>
+struct InterpSys {
+    InterpArgs<T> args;
+};
+// All systems in one persistent launch over their tiles (prefix as for the
+// spread; smem = the largest interp_smem_bytes of the systems).
+template <typename T>
+cudaError_t launch_interp_batch(const InterpSys<T> *sys, const int *prefix, int nsys, int total,
+                                size_t smem, cudaStream_t s);
 // Components [cb, ce) of the C-component mesh (cb a multiple of 4) into
 // W[n][C]; err: device flag set to 1 if a TMA wait timed out.
 template <typename T>
@@ -81,6 +129,10 @@ cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, co
                           const uint32_t *rec_start, const T *rec_w, const T *mesh, int C,
                           int cb, int ce, const MeshGeom &g, T *W, int accumulate, int *err,
                           cudaStream_t s);
+
+// ---- host tables (engine.cu) ----------------------------------------------
+// |b(m)|^2 = 1 / |sum_{j<p-1} M_p(j+1) e^{i j 2 pi m'/K}|^2 (old-version/spme.c:109-126).
+void host_moduli2(int K, int p, std::vector<double> &out);
 
 // ---- k-space influence (influence.cu) -------------------------------------
 // tab[(z*K + y)*Kh + kx] = (S(k)|b|^2 / V, S(k)|b|^2 / (V k^2)), zero at k = 0.
@@ -151,6 +203,28 @@ template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
                              const T *F, int R, double L, double rc, double xi, double a,
                              int with_self, const PairTable &tab, T *W, cudaStream_t s);
+// Arguments of one system's real-space sum (cell_off indexed by this system's
+// cells; slots, positions and rows global).
+template <typename T>
+struct RealArgs {
+    const int *cell_off;
+    const int *cell_perm;
+    const void *cpos;
+    const T *F;
+    T *W;
+    int nc, R, with_self;
+    double L, h, rc2, xi, a, self_c;
+    PairTable tab;
+};
+double real_self_coeff(double xi, double a);
+template <typename T>
+RealArgs<T> real_args(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
+                      const T *F, int R, double L, double rc, double xi, double a, int with_self,
+                      const PairTable &tab, T *W);
+// All systems in one persistent launch over their cells (prefix as for the spread).
+template <typename T>
+cudaError_t launch_realspace_batch(const RealArgs<T> *sys, const int *prefix, int nsys,
+                                   int total, cudaStream_t s);
 
 // ---- layout conversions (pack.cu) -----------------------------------------
 // W = self_c * F (the self term alone, when no real-space sum is requested)

@@ -9,6 +9,7 @@
 // candidates of the 27 neighbour cells (details at the kernel below).
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.h"
@@ -188,11 +189,18 @@ constexpr int kCap = 512;  // candidates staged in shared memory per cell
 // FP32: 64 registers, 16 blocks (32 warps) per SM (measured faster than the
 // unconstrained 80 registers); FP64 needs more registers.
 template <typename T, typename G>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 16 : 8)
-k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ cell_perm,
-            const typename Geo4<G>::type *__restrict__ cpos, const T *__restrict__ F, int R,
-            G L, G h, G rc2, T xi, T a, T self_c, int with_self, PairTable tab,
-            T *__restrict__ W) {
+__device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
+    const int nc = A.nc;
+    const int *__restrict__ cell_off = A.cell_off;
+    const int *__restrict__ cell_perm = A.cell_perm;
+    const typename Geo4<G>::type *__restrict__ cpos =
+        reinterpret_cast<const typename Geo4<G>::type *>(A.cpos);
+    const T *__restrict__ F = A.F;
+    T *__restrict__ W = A.W;
+    const int R = A.R, with_self = A.with_self;
+    const G L = (G)A.L, h = (G)A.h, rc2 = (G)A.rc2;
+    const T xi = (T)A.xi, a = (T)A.a, self_c = (T)A.self_c;
+    const PairTable &tab = A.tab;
     __shared__ int nb_beg[27], nb_pre[28], nnb;
     __shared__ G nb_shift[27][3];
     __shared__ G cx[kCap], cy[kCap], cz[kCap];
@@ -212,7 +220,6 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
     __shared__ PairRec prec[kWarps][32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int cell = blockIdx.x;
     const int C = 3 * R;
     if (tid == 0) {
         const int ccx = cell % nc, ccy = (cell / nc) % nc, ccz = cell / (nc * nc);
@@ -410,26 +417,93 @@ k_realspace(int nc, const int *__restrict__ cell_off, const int *__restrict__ ce
     }
 }
 
+template <typename T, typename G>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 16 : 8) k_realspace(RealArgs<T> A) {
+    realspace_body<T, G>(A, blockIdx.x);
+}
+
+// Many systems in one persistent launch over their cells.
+template <typename T, typename G>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 16 : 8)
+k_realspace_batch(const RealArgs<T> *__restrict__ sys, const int *__restrict__ prefix, int nsys,
+                  int total) {
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int k = batch_find(prefix, nsys, w);
+        const RealArgs<T> A = sys[k];
+        realspace_body<T, G>(A, w - prefix[k]);
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+double real_self_coeff(double xi, double a) {
+    const double rsp = 0.56418958354775628695;
+    return (1.0 - 6.0 * xi * a * rsp + 40.0 / 3.0 * xi * xi * xi * a * a * a * rsp) / a;
+}
+
+template <typename T>
+RealArgs<T> real_args(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
+                      const T *F, int R, double L, double rc, double xi, double a, int with_self,
+                      const PairTable &tab, T *W) {
+    RealArgs<T> A;
+    A.nc = nc;
+    A.cell_off = cell_off;
+    A.cell_perm = cell_perm;
+    A.cpos = cpos;
+    A.F = F;
+    A.W = W;
+    A.R = R;
+    A.with_self = with_self;
+    A.L = L;
+    A.h = L / nc;
+    A.rc2 = rc * rc;
+    A.xi = xi;
+    A.a = a;
+    A.self_c = real_self_coeff(xi, a);
+    A.tab = tab;
+    return A;
+}
 
 template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
                              const T *F, int R, double L, double rc, double xi, double a,
                              int with_self, const PairTable &tab, T *W, cudaStream_t s) {
-    const double rsp = 0.56418958354775628695;
-    const double self_c = (1.0 - 6.0 * xi * a * rsp + 40.0 / 3.0 * xi * xi * xi * a * a * a * rsp) / a;
     const int ncell = nc * nc * nc;
-    const double h = L / nc;
+    const RealArgs<T> A = real_args<T>(nc, cell_off, cell_perm, cpos, F, R, L, rc, xi, a,
+                                       with_self, tab, W);
     if constexpr (sizeof(T) == 8)
-        k_realspace<T, double><<<ncell, kThreads, 0, s>>>(
-            nc, cell_off, cell_perm, (const double4 *)cpos, F, R, L, h, rc * rc, (T)xi, (T)a,
-            (T)self_c, with_self, tab, W);
+        k_realspace<T, double><<<ncell, kThreads, 0, s>>>(A);
     else
-        k_realspace<T, float><<<ncell, kThreads, 0, s>>>(
-            nc, cell_off, cell_perm, (const float4 *)cpos, F, R, (float)L, (float)h,
-            (float)(rc * rc), (T)xi, (T)a, (T)self_c, with_self, tab, W);
+        k_realspace<T, float><<<ncell, kThreads, 0, s>>>(A);
     return cudaGetLastError();
 }
+
+template <typename T>
+cudaError_t launch_realspace_batch(const RealArgs<T> *sys, const int *prefix, int nsys,
+                                   int total, cudaStream_t s) {
+    if (total <= 0) return cudaSuccess;
+    using G = typename std::conditional<sizeof(T) == 8, double, float>::type;
+    auto kern = k_realspace_batch<T, G>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
+    const int grid = std::max(1, std::min(total, sms * std::max(per_sm, 1)));
+    kern<<<grid, kThreads, 0, s>>>(sys, prefix, nsys, total);
+    return cudaGetLastError();
+}
+
+template RealArgs<float> real_args<float>(int, const int *, const int *, const void *,
+                                          const float *, int, double, double, double, double, int,
+                                          const PairTable &, float *);
+template RealArgs<double> real_args<double>(int, const int *, const int *, const void *,
+                                            const double *, int, double, double, double, double,
+                                            int, const PairTable &, double *);
+template cudaError_t launch_realspace_batch<float>(const RealArgs<float> *, const int *, int, int,
+                                                   cudaStream_t);
+template cudaError_t launch_realspace_batch<double>(const RealArgs<double> *, const int *, int,
+                                                    int, cudaStream_t);
 
 template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,

@@ -30,6 +30,7 @@
 //   * the block's columns are transposed through shared memory and written as
 //     whole mesh rows (coalesced), once: no zeroing, no atomics.
 // Mesh layout: component-major mesh[c][z][y][x] (the cuFFT batch layout).
+#include <algorithm>
 #include <utility>
 
 #include "kernels.h"
@@ -162,14 +163,20 @@ struct WarpScratch {
     int pre[NQ + 1];
 };
 
+// One block's work: columns [bx XT, bx XT + XT) of row y = by, z tile and
+// component chunk bz (nzt z tiles per chunk).  Runs as the body of the
+// single-system kernel and of the batched one.
 template <typename T, int P, int CPL, int TZ, int NW>
-__global__ void __launch_bounds__(NW * 32, (sizeof(T) == 4 ? 3 : 1))
-k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_start,
-              const T *__restrict__ rec_w, const T *__restrict__ Fs, int C, int RW, int K,
-              int nzt, T *__restrict__ mesh) {
+__device__ __forceinline__ void spread_cols_body(const SpreadColsArgs<T> &A, int bx, int by,
+                                                 int bz) {
     constexpr bool F32 = sizeof(T) == 4;
-    constexpr int WS = RecordWidth<T, P>::value;
     constexpr int WR = WRow<T, P>::value;
+    const int *__restrict__ soff = A.soff;
+    const uint32_t *__restrict__ rec_start = A.rec_start;
+    const T *__restrict__ rec_w = A.rec_w;
+    const T *__restrict__ Fs = A.Fs;
+    T *__restrict__ mesh = A.mesh;
+    const int C = A.C, RW = A.RW, K = A.K, nzt = A.nzt, WS = A.ws;
     constexpr int PC = cols_pcpl(CPL);  // padded components per lane in a force row
     constexpr int XT = 2 * NW;          // columns per block
     constexpr int CC = 16 * CPL;        // components per block
@@ -189,9 +196,9 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
     T *tsm = reinterpret_cast<T *>(sp_raw);  // [CC][ROW] transpose buffer
     const size_t tsm_bytes = ((size_t)CC * ROW * sizeof(T) + 15) & ~(size_t)15;
 
-    const int x0 = blockIdx.x * XT;
-    const int y = blockIdx.y;
-    const int zt = blockIdx.z % nzt, chunk = blockIdx.z / nzt;
+    const int x0 = bx * XT;
+    const int y = by;
+    const int zt = bz % nzt, chunk = bz / nzt;
     const int z0 = zt * TZ;
     const int ext = min(TZ, K - z0);
     const int cb = chunk * CC;
@@ -404,6 +411,24 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
     constexpr int CSTEP = (NW * 32) >= SLOTS ? (NW * 32) / SLOTS : 1;  // components per sweep
     const size_t K3 = (size_t)K * K * K;
     const int nc = min(CC, C - cb);
+    if constexpr (F32) {
+        // even K: pairs of columns per thread (8-byte loads and stores; ROW is even)
+        if ((K & 1) == 0) {
+            constexpr int SL2 = XT * TZ / 2;  // (plane, column pair) slots of a component
+            constexpr int CS2 = (NW * 32) >= SL2 ? (NW * 32) / SL2 : 1;
+            static_assert(ROW % 2 == 0, "pair loads from the transpose buffer");
+            for (int slot = threadIdx.x % SL2; slot < SL2; slot += NW * 32) {
+                const int z = slot / (XT / 2), x = 2 * (slot - z * (XT / 2));
+                if (z >= ext || x0 + x >= K) continue;  // K, x0 + x even: x0 + x + 1 < K
+                float2 *out = reinterpret_cast<float2 *>(
+                    mesh + (size_t)cb * K3 + ((size_t)(z0 + z) * K + y) * K + x0 + x);
+                const float2 *src = reinterpret_cast<const float2 *>(tsm + z * XT + x);
+                for (int c = threadIdx.x / SL2; c < nc; c += CS2)
+                    out[(size_t)c * (K3 / 2)] = src[(size_t)c * (ROW / 2)];
+            }
+            return;
+        }
+    }
     for (int slot = threadIdx.x % SLOTS; slot < SLOTS; slot += NW * 32) {
         const int z = slot / XT, x = slot - z * XT;
         if (z >= ext || x0 + x >= K) continue;
@@ -411,6 +436,34 @@ k_spread_cols(const int *__restrict__ soff, const uint32_t *__restrict__ rec_sta
         const T *src = tsm + z * XT + x;
         for (int c = threadIdx.x / SLOTS; c < nc; c += CSTEP)
             out[(size_t)c * K3] = src[(size_t)c * ROW];
+    }
+}
+
+template <typename T, int P, int CPL, int TZ, int NW>
+__global__ void __launch_bounds__(NW * 32, (sizeof(T) == 4 ? 3 : 1))
+k_spread_cols(SpreadColsArgs<T> A) {
+    spread_cols_body<T, P, CPL, TZ, NW>(A, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Many systems in one persistent launch: work item w (a block of one system)
+// -> system k with prefix[k] <= w < prefix[k + 1]; the order p of each system
+// selects the body.
+template <typename T, int CPL, int TZ, int NW>
+__global__ void __launch_bounds__(NW * 32, (sizeof(T) == 4 ? 3 : 1))
+k_spread_cols_batch(const SpreadColsSys<T> *__restrict__ sys, const int *__restrict__ prefix,
+                    int nsys, int total) {
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int k = batch_find(prefix, nsys, w);
+        const SpreadColsSys<T> S = sys[k];
+        const int local = w - prefix[k];
+        const int bx = local % S.gx, rest = local / S.gx;
+        const int by = rest % S.args.K, bz = rest / S.args.K;
+        switch (S.p) {
+            case 4: spread_cols_body<T, 4, CPL, TZ, NW>(S.args, bx, by, bz); break;
+            case 6: spread_cols_body<T, 6, CPL, TZ, NW>(S.args, bx, by, bz); break;
+            default: spread_cols_body<T, 8, CPL, TZ, NW>(S.args, bx, by, bz); break;
+        }
+        __syncthreads();  // shared memory is reused by the next work item
     }
 }
 
@@ -452,8 +505,30 @@ cudaError_t launch_cols(const int *soff, const uint32_t *rec_start, const T *rec
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((K + XT - 1) / XT, K, nzt * nchunk);
-    kern<<<grid, NW * 32, smem, s>>>(soff, rec_start, rec_w, Fs, C, spread_cols_row_width(C), K,
-                                     nzt, mesh);
+    SpreadColsArgs<T> A{soff, rec_start, rec_w, Fs, mesh, C, spread_cols_row_width(C), K, nzt,
+                        RecordWidth<T, P>::value};
+    kern<<<grid, NW * 32, smem, s>>>(A);
+    return cudaGetLastError();
+}
+
+template <typename T, int CPL>
+cudaError_t launch_cols_batch(const SpreadColsSys<T> *sys, const int *prefix, int nsys,
+                              int total, cudaStream_t s) {
+    constexpr int NW = 8;
+    constexpr int TZ = sizeof(T) == 4 ? 16 : 8;
+    constexpr int XT = 2 * NW, CC = 16 * CPL;
+    const size_t smem = (((size_t)CC * (TZ * XT + (sizeof(T) == 4 ? 2 : 1)) * sizeof(T) + 15) &
+                         ~(size_t)15) +
+                        NW * sizeof(WarpScratch<T, 8>);  // the largest order's scratch
+    auto kern = k_spread_cols_batch<T, CPL, TZ, NW>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NW * 32, smem);
+    const int grid = std::max(1, std::min(total, sms * std::max(per_sm, 1)));
+    kern<<<grid, NW * 32, smem, s>>>(sys, prefix, nsys, total);
     return cudaGetLastError();
 }
 
@@ -475,13 +550,14 @@ int blocks_for_rows(size_t total) {
 
 }  // namespace
 
-// The z runs of one tile must not wrap onto themselves (TZ + p - 1 <= K) and
-// the p + 1 start columns of a column pair must be distinct: K >= 32 covers
-// both for p <= 8.  Any number of components (the cost is per visit: below 16
-// components lanes idle, but the tile kernel's wasted visits cost more).
-bool spread_cols_ok(int K, int C, size_t elem) {
-    (void)elem;
-    return K >= 32 && K <= 1024 && C >= 1;
+// The z runs of one tile must not wrap onto themselves (TZ + p - 1 <= K, TZ =
+// 16 planes in FP32, 8 in FP64) and the p + 1 start columns of a column pair
+// must be distinct (K >= p + 1).  Any number of components (the cost is per
+// visit: below 16 components lanes idle, but the tile kernel's wasted visits
+// cost more).
+bool spread_cols_ok(int K, int C, size_t elem, int p) {
+    const int TZ = elem == 4 ? 16 : 8;
+    return K >= TZ + p - 1 && K >= p + 1 && K <= 1024 && C >= 1;
 }
 
 int spread_cols_row_width(int C) {
@@ -512,7 +588,7 @@ void launch_gather_cols_rows(const T *F, const int *idx, int n, int C, T *Fs, cu
 template <typename T>
 cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, const T *rec_w,
                                const T *Fs, int C, const MeshGeom &g, T *mesh, cudaStream_t s) {
-    if (!spread_cols_ok(g.K, C, sizeof(T))) return cudaErrorInvalidValue;
+    if (!spread_cols_ok(g.K, C, sizeof(T), g.p)) return cudaErrorInvalidValue;
     switch (g.p) {
         case 4: return dispatch_cpl<T, 4>(start_off, rec_start, rec_w, Fs, C, g, mesh, s);
         case 6: return dispatch_cpl<T, 6>(start_off, rec_start, rec_w, Fs, C, g, mesh, s);
@@ -521,6 +597,26 @@ cudaError_t launch_spread_cols(const int *start_off, const uint32_t *rec_start, 
     }
 }
 
+template <typename T>
+cudaError_t launch_spread_cols_batch(const SpreadColsSys<T> *sys, const int *prefix, int nsys,
+                                     int total, int C, cudaStream_t s) {
+    if (total <= 0) return cudaSuccess;
+    switch (cols_cpl(C)) {
+        case 1: return launch_cols_batch<T, 1>(sys, prefix, nsys, total, s);
+        case 2: return launch_cols_batch<T, 2>(sys, prefix, nsys, total, s);
+        default: return launch_cols_batch<T, 3>(sys, prefix, nsys, total, s);
+    }
+}
+
+int spread_cols_blocks(int K, int C, size_t elem) {
+    const int TZ = elem == 4 ? 16 : 8, XT = 16, CC = 16 * cols_cpl(C);
+    return ((K + XT - 1) / XT) * K * ((K + TZ - 1) / TZ) * ((C + CC - 1) / CC);
+}
+
+template cudaError_t launch_spread_cols_batch<float>(const SpreadColsSys<float> *, const int *,
+                                                     int, int, int, cudaStream_t);
+template cudaError_t launch_spread_cols_batch<double>(const SpreadColsSys<double> *, const int *,
+                                                      int, int, int, cudaStream_t);
 template void launch_gather_cols_rows<float>(const float *, const int *, int, int, float *,
                                              cudaStream_t);
 template void launch_gather_cols_rows<double>(const double *, const int *, int, int, double *,
