@@ -522,7 +522,10 @@ def run_gb300(args, w):
 
 
 def run_batch(args, w):
-    """Uneven batch: all systems in one captured graph vs a per-system loop."""
+    """Uneven batch: the native batch (one persistent launch per stage over all
+    systems, one cuFFT plan per distinct K, the step one CUDA-graph launch)
+    against the same systems through one engine each (a per-system loop, and
+    the engines as branches of one captured graph)."""
     import torch
 
     from spme_gb300.batch import SystemBatch, uneven_systems
@@ -537,33 +540,39 @@ def run_batch(args, w):
     f = [torch.tensor(rng.standard_normal((R, 3 * s["N"])), dtype=torch.float32, device="cuda")
          for s in systems]
     u = [torch.zeros_like(x) for x in f]
-    b = SystemBatch(systems, nrhs=R)
+    b = SystemBatch(systems, nrhs=R)  # autotunes the batch's tile and concurrency in bind
     b.bind(pos, f, u)
     units = sum(s["N"] for s in systems) * R
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        b.run_loop()
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        b.run_loop()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    loop_ms = e0.elapsed_time(e1) / args.steps
-    b.capture()
-    for _ in range(args.warmup):
-        b.run()
-    torch.cuda.synchronize()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    loop_ms = timed(b.run_loop)
+    b.capture_engines_graph()
+    graph_ms = timed(b.run_engines_graph)
+    l0 = b.batch.launch_count()
     clocks = Clocks(local)
     clocks.start()
-    e0.record(b._main)
-    for _ in range(args.steps):
-        b.run()
-    e1.record(b._main)
-    torch.cuda.synchronize()
+    ms = timed(b.run)
     ck = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    launches = (b.batch.launch_count() - l0) // (args.steps + args.warmup)
+    # one serialized step attributes time to every stage
+    b.batch.set_graphs(False)
+    b.batch.set_profiling(True)
+    b.run()
+    torch.cuda.synchronize()
+    stages = b.batch.stage_times()
+    b.batch.set_profiling(False)
     if rank != 0:
         return 0
     line = {
@@ -575,10 +584,15 @@ def run_batch(args, w):
                                f"[500, 50000], phi=0.05, K=next smooth >= 0.6 L, p in {{4,6,8}}, "
                                f"R={R}, xi={w['xi']}, rc={w['rc']}",
                    "systems": len(systems), "particles": units // R,
+                   "distinct_K": len({s["K"] for s in systems}),
                    "l2": "whole batch larger than L2"},
+        "gpu_launches": launches,
+        "stages_ms_serialized": stages,
         "per_system_loop": {"value": loop_ms * 1e6 / units, "unit": UNIT, "ms_per_step": loop_ms},
-        "graph_speedup_vs_loop": loop_ms / ms,
-        "tiles": {f"N{s['N']}_K{s['K']}_p{s['p']}": list(t) for s, t in zip(systems, b.tiles)},
+        "engines_graph": {"value": graph_ms * 1e6 / units, "unit": UNIT, "ms_per_step": graph_ms},
+        "speedup_vs_loop": loop_ms / ms,
+        "speedup_vs_engines_graph": graph_ms / ms,
+        "autotune": ({"tile": list(b.tuned[0]), "overlap": b.tuned[1]} if b.tuned else None),
         "clocks": ck,
     }
     print(json.dumps(line), flush=True)

@@ -174,6 +174,64 @@ int spme_read_xyz(const char *path, int *np, double *box_size, double **pos, dou
 int spme_write_xyz(const char *path, int np, double box_size, const double *pos, double radius);
 void spme_free(void *p);
 
+/* ---- batches of independent systems --------------------------------------
+ * No counterpart in the reference (its compute_spme, old-version/spme.c:560-726,
+ * applies one system).  A batch holds systems of different size N_k, box L_k,
+ * mesh K_k and order p_k with the same number of right-hand sides R and
+ * precision, and applies the full operator M_k = M_recip + M_real + M_self to
+ * each of them; every stage (position build, spread, influence,
+ * interpolation, real-space sum, layout conversions) is one launch over a
+ * packed work list of all systems, and cuFFT runs one batched plan per
+ * distinct K.  Device pointers only; work ordered on the batch's stream.
+ *
+ * Packed layouts (systems in the order given, P_k = N_0 + ... + N_{k-1}):
+ *   positions: system k's N_k x 3 doubles at element 3 P_k;
+ *   vectors:   system k's R right-hand sides at element 3 R P_k, right-hand
+ *              side r of particle i, Cartesian d at 3 R P_k + r 3 N_k + 3 i + d
+ *              (compute_spme's layout with ld = 3 N_k, per system).
+ * Each system needs K >= p + 15 (FP32) or K >= p + 7 (FP64), rc < L/2. */
+typedef struct spme_batch_system {
+    int np;
+    int dim;
+    int porder;
+    double box_size;
+    double xi;
+    double radius;
+    double rcut;
+} spme_batch_system;
+
+typedef struct _spme_batch_t spme_batch_t;
+
+int spme_batch_create(const spme_batch_system *systems, int count, int nrhs, int precision,
+                      spme_batch_t **out);
+int spme_batch_destroy(spme_batch_t *batch);
+/* A batch starts on a non-blocking stream of its own (spme_batch_get_stream);
+ * NULL selects the legacy default stream, as for spme_set_stream. */
+int spme_batch_set_stream(spme_batch_t *batch, void *stream);
+void *spme_batch_get_stream(const spme_batch_t *batch);
+/* Interpolation tile of every system (as spme_set_tile, default 16 x 8 x 4);
+ * positions must be set again. */
+int spme_batch_set_tile(spme_batch_t *batch, int tx, int ty, int tz);
+int spme_batch_set_positions(spme_batch_t *batch, const double *pos);
+/* u = beta u + alpha M f for every system (packed layouts above). */
+int spme_batch_apply(spme_batch_t *batch, double alpha, const void *f, double beta, void *u);
+/* set_positions + apply; with graphs on, captured once per (pointers, alpha,
+ * beta, stream) and replayed as one CUDA graph launch. */
+int spme_batch_step(spme_batch_t *batch, const double *pos, double alpha, const void *f,
+                    double beta, void *u);
+int spme_batch_set_graphs(spme_batch_t *batch, int on);
+/* Concurrency inside a step (OR of): 1 the real-space sum on a second stream
+ * beside the mesh pipeline, 2 the cuFFT groups on four streams.  Default 0. */
+int spme_batch_set_overlap(spme_batch_t *batch, int mode);
+int spme_batch_synchronize(spme_batch_t *batch);
+long spme_batch_launch_count(const spme_batch_t *batch);
+long spme_batch_particles(const spme_batch_t *batch);
+/* Per-stage device times (ms) of the last uncaptured step with profiling on:
+ * position build, pack, real-space, spread, forward FFT, influence, backward
+ * FFT, interpolate, unpack.  Returns the number written (<= n). */
+int spme_batch_set_profiling(spme_batch_t *batch, int on);
+int spme_batch_stage_times(const spme_batch_t *batch, float *ms, int n);
+
 /* Real-space + self mobility apply that allocates no device memory.
  * No counterpart in the reference (which has no real-space term).  For callers
  * that cannot call cudaMalloc: applications that reserve all device memory in

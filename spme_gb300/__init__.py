@@ -57,6 +57,20 @@ class Params(ctypes.Structure):
     ]
 
 
+class BatchSystem(ctypes.Structure):
+    """Mirror of ``spme_batch_system`` (include/spme_gb300.h)."""
+
+    _fields_ = [
+        ("np", ctypes.c_int),
+        ("dim", ctypes.c_int),
+        ("porder", ctypes.c_int),
+        ("box_size", ctypes.c_double),
+        ("xi", ctypes.c_double),
+        ("radius", ctypes.c_double),
+        ("rcut", ctypes.c_double),
+    ]
+
+
 def load(path: str | None = None):
     """Load libspme_gb300.so (raises if it is absent: no fallback path exists)."""
     global _lib
@@ -98,6 +112,21 @@ def load(path: str | None = None):
                               ctypes.POINTER(ctypes.POINTER(d)), ctypes.POINTER(ctypes.POINTER(d))]),
         "spme_write_xyz": (i, [ctypes.c_char_p, i, d, _P, d]),
         "spme_free": (None, [_P]),
+        "spme_batch_create": (i, [ctypes.POINTER(BatchSystem), i, i, i, ctypes.POINTER(_P)]),
+        "spme_batch_destroy": (i, [_P]),
+        "spme_batch_set_stream": (i, [_P, _P]),
+        "spme_batch_get_stream": (_P, [_P]),
+        "spme_batch_set_tile": (i, [_P, i, i, i]),
+        "spme_batch_set_positions": (i, [_P, _P]),
+        "spme_batch_apply": (i, [_P, d, _P, d, _P]),
+        "spme_batch_step": (i, [_P, _P, d, _P, d, _P]),
+        "spme_batch_set_graphs": (i, [_P, i]),
+        "spme_batch_set_overlap": (i, [_P, i]),
+        "spme_batch_synchronize": (i, [_P]),
+        "spme_batch_launch_count": (l, [_P]),
+        "spme_batch_particles": (l, [_P]),
+        "spme_batch_set_profiling": (i, [_P, i]),
+        "spme_batch_stage_times": (i, [_P, ctypes.POINTER(ctypes.c_float), i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -347,3 +376,107 @@ class Engine:
 
     def launch_count(self) -> int:
         return int(load().spme_launch_count(self.h))
+
+
+class Batch:
+    """Independent systems (uneven N, L, K, p; same right-hand-side count and
+    precision) applied together: every stage is one launch over a packed work
+    list of all systems, cuFFT one batched plan per distinct K
+    (``spme_batch_*`` in include/spme_gb300.h).  Device (CUDA tensor) data only,
+    in the packed layouts: positions ``pack(pos_list)`` (sum N x 3 float64),
+    vectors ``pack(f_list)`` with system k's (R, 3 N_k) rows contiguous.  Work
+    is ordered on torch's current stream."""
+
+    STAGES = ("positions", "pack", "realspace", "spread", "fft_fwd", "influence", "fft_bwd",
+              "interp", "unpack")
+
+    def __init__(self, systems: list, nrhs: int = 4, precision: str = "fp32"):
+        lib = load()
+        arr = (BatchSystem * len(systems))()
+        for k, sy in enumerate(systems):
+            arr[k].np, arr[k].dim, arr[k].porder = int(sy["N"]), int(sy["K"]), int(sy["p"])
+            arr[k].box_size, arr[k].xi = float(sy["L"]), float(sy["xi"])
+            arr[k].radius, arr[k].rcut = float(sy.get("radius", 1.0)), float(sy["rc"])
+        h = _P()
+        prec = SPME_FP32 if precision == "fp32" else SPME_FP64
+        _check(lib.spme_batch_create(arr, len(systems), int(nrhs), prec, ctypes.byref(h)),
+               "spme_batch_create")
+        self.h = h
+        self.systems = list(systems)
+        self.nrhs = int(nrhs)
+        self.dtype = np.float32 if precision == "fp32" else np.float64
+        self._stream = lib.spme_batch_get_stream(h)
+
+    @staticmethod
+    def pack(parts):
+        """Concatenate per-system tensors (positions (N_k, 3) or vectors (R, 3 N_k))."""
+        import torch
+        return torch.cat([x.reshape(-1) for x in parts])
+
+    def unpack(self, packed):
+        """Per-system views (R, 3 N_k) of a packed vector."""
+        out, off = [], 0
+        for sy in self.systems:
+            m = self.nrhs * 3 * int(sy["N"])
+            out.append(packed[off:off + m].view(self.nrhs, 3 * int(sy["N"])))
+            off += m
+        return out
+
+    def _follow_torch(self):
+        import torch
+        cur = torch.cuda.current_stream().cuda_stream or None
+        if cur != self._stream:
+            _check(load().spme_batch_set_stream(self.h, cur), "spme_batch_set_stream")
+            self._stream = cur
+
+    def set_positions(self, pos):
+        self._follow_torch()
+        _check(load().spme_batch_set_positions(self.h, pos.data_ptr()), "spme_batch_set_positions")
+
+    def apply(self, f, u, alpha: float = 1.0, beta: float = 0.0):
+        self._follow_torch()
+        _check(load().spme_batch_apply(self.h, alpha, f.data_ptr(), beta, u.data_ptr()),
+               "spme_batch_apply")
+        return u
+
+    def step(self, pos, f, u, alpha: float = 1.0, beta: float = 0.0):
+        """Positions then apply; one CUDA graph launch when graphs are on."""
+        self._follow_torch()
+        _check(load().spme_batch_step(self.h, pos.data_ptr(), alpha, f.data_ptr(), beta,
+                                      u.data_ptr()), "spme_batch_step")
+        return u
+
+    def set_graphs(self, on: bool = True):
+        _check(load().spme_batch_set_graphs(self.h, 1 if on else 0), "spme_batch_set_graphs")
+
+    def set_tile(self, tx: int, ty: int, tz: int):
+        _check(load().spme_batch_set_tile(self.h, tx, ty, tz), "spme_batch_set_tile")
+
+    def set_overlap(self, mode: int):
+        """1: real-space sum on a second stream; 2: cuFFT groups on four streams."""
+        _check(load().spme_batch_set_overlap(self.h, int(mode)), "spme_batch_set_overlap")
+
+    def set_profiling(self, on: bool = True):
+        load().spme_batch_set_profiling(self.h, 1 if on else 0)
+
+    def stage_times(self) -> dict:
+        buf = (ctypes.c_float * len(self.STAGES))()
+        n = load().spme_batch_stage_times(self.h, buf, len(self.STAGES))
+        return {self.STAGES[k]: float(buf[k]) for k in range(n)}
+
+    def synchronize(self):
+        _check(load().spme_batch_synchronize(self.h), "spme_batch_synchronize")
+
+    def launch_count(self) -> int:
+        return int(load().spme_batch_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().spme_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

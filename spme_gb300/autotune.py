@@ -98,3 +98,52 @@ def autotune(engine, pos, f, reps: int = 3, candidates=None, use_cache: bool = T
         cache[key] = {"tile": list(best), "ms": {"x".join(map(str, k)): v for k, v in timings.items()}}
         _save_cache(path, cache)
     return best, timings
+
+
+BATCH_TILES = [(16, 8, 4), (8, 8, 8), (8, 8, 4), (16, 8, 8), (16, 16, 4)]
+BATCH_OVERLAP = [0, 1, 2, 3]
+
+
+def autotune_batch(batch, pos, f, u, reps: int = 3, tiles=None, overlaps=None) -> tuple:
+    """Pick the interpolation tile (every system on the same tile) and the
+    in-step concurrency (real-space sum on a second stream, cuFFT groups on
+    four streams) of a native batch: each candidate times a few batched steps
+    (CUDA events on torch's current stream).  Leaves the batch on the chosen
+    settings.  Returns ((tile, overlap), {(tile, overlap): ms per step})."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+
+    def time_steps():
+        batch.step(pos, f, u)  # capture (graphs on) and warm-up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            batch.step(pos, f, u)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    timings = {}
+    for tile in tiles or BATCH_TILES:
+        try:
+            batch.set_tile(*tile)
+            batch.set_overlap(0)
+            timings[(tile, 0)] = time_steps()
+        except Exception:
+            continue
+    if not timings:
+        raise RuntimeError("no tile candidate ran")
+    best_tile = min(timings, key=timings.get)[0]
+    batch.set_tile(*best_tile)
+    for ov in overlaps or BATCH_OVERLAP:
+        if (best_tile, ov) in timings:
+            continue
+        batch.set_overlap(ov)
+        timings[(best_tile, ov)] = time_steps()
+    best = min(timings, key=timings.get)
+    batch.set_tile(*best[0])
+    batch.set_overlap(best[1])
+    batch.step(pos, f, u)
+    torch.cuda.synchronize()
+    return best, timings

@@ -1,17 +1,17 @@
-"""Uneven batches of independent systems in one CUDA-graph launch.
+"""Uneven batches of independent systems.
 
 A batch holds systems of different N, box L, mesh K and order p (e.g. 64
 systems with N between 500 and 50,000).  Each system is small: alone, its
-spread launch may cover a few dozen tiles and leave most of the 152 SMs idle,
-and a per-system loop pays ~20 launches per system.  Here every system keeps
-its own engine (own streams, tiles picked by the autotuner) and the whole
-batch — position builds and applies of all systems — is captured once into a
-single CUDA graph in which the systems are independent branches; one graph
-launch then runs them concurrently and fills the GPU.
+kernels cover a few dozen tiles and leave most of the 152 SMs idle, and a
+per-system loop pays ~20 launches per system.
 
-cuFFT cannot run inside a persistent kernel, so the batch is a graph of
-per-system kernels rather than one persistent kernel; the graph gives the
-same single launch and concurrency.
+``SystemBatch.run`` uses the native batch (:class:`spme_gb300.Batch`,
+``spme_batch_*`` in include/spme_gb300.h): every stage of the position build
+and of the apply is one persistent launch over a packed work list of all
+systems' blocks, cuFFT runs one batched plan per distinct K, and the whole
+step is one captured CUDA graph.  Two references run the same systems through
+separate engines: ``run_loop`` one after the other, ``run_engines_graph`` as
+independent branches of one captured graph.
 """
 from __future__ import annotations
 
@@ -19,7 +19,7 @@ import math
 
 import numpy as np
 
-from . import TERM_ALL, Engine, next_smooth
+from . import TERM_ALL, Batch, Engine, next_smooth
 
 
 def uneven_systems(count: int = 64, nmin: int = 500, nmax: int = 50_000, phi: float = 0.05,
@@ -43,28 +43,49 @@ class SystemBatch:
 
     ``bind(pos, f, u)`` fixes the device buffers (lists of CUDA tensors:
     positions (N_i, 3) float64, right-hand sides (R, 3 N_i) and outputs of the
-    engine precision); ``capture()`` records one graph; ``run()`` replays it
-    (positions rebuilt and all systems applied); ``run_loop()`` is the
-    sequential per-system reference."""
+    batch precision) and packs them; ``run()`` is one native batched step
+    (positions rebuilt, all systems applied, one graph launch) into the packed
+    result, ``results()`` its per-system views; ``run_loop()`` and
+    ``run_engines_graph()`` write the caller's ``u`` tensors through one engine
+    per system."""
 
     def __init__(self, systems: list[dict], nrhs: int = 4, precision: str = "fp32",
                  terms: int = TERM_ALL, tune: bool = True):
+        if terms != TERM_ALL:
+            raise ValueError("a batch applies the full operator (TERM_ALL)")
         self.systems = systems
         self.nrhs = nrhs
+        self.precision = precision
         self.tune = tune
-        self.engines = [Engine(s["N"], s["L"], s["xi"], s["K"], s["p"], radius=s["radius"],
-                               rcut=s["rc"], precision=precision, max_nrhs=nrhs, terms=terms)
-                        for s in systems]
+        self.batch = Batch(systems, nrhs=nrhs, precision=precision)
+        self.batch.set_graphs(True)
+        self.engines = None
         self.graph = None
-        self.tiles = [None] * len(systems)
+        self.tuned = None
+
+    def _make_engines(self):
+        if self.engines is None:
+            self.engines = [Engine(s["N"], s["L"], s["xi"], s["K"], s["p"], radius=s["radius"],
+                                   rcut=s["rc"], precision=self.precision, max_nrhs=self.nrhs,
+                                   terms=TERM_ALL) for s in self.systems]
 
     def bind(self, pos, f, u):
+        import torch
         self.pos, self.f, self.u = list(pos), list(f), list(u)
+        self.pos_p = Batch.pack(self.pos).contiguous()
+        self.f_p = Batch.pack(self.f).contiguous()
+        self.u_p = torch.zeros_like(self.f_p)
         self.graph = None
         if self.tune:
-            from .autotune import autotune
-            for k, eng in enumerate(self.engines):
-                self.tiles[k], _ = autotune(eng, self.pos[k], self.f[k], reps=2)
+            from .autotune import autotune_batch
+            self.tuned, _ = autotune_batch(self.batch, self.pos_p, self.f_p, self.u_p)
+
+    def run(self):
+        """One batched step (one CUDA graph launch after the first call)."""
+        self.batch.step(self.pos_p, self.f_p, self.u_p)
+
+    def results(self):
+        return self.batch.unpack(self.u_p)
 
     def _apply_one(self, k):
         self.engines[k].set_positions(self.pos[k])
@@ -72,11 +93,14 @@ class SystemBatch:
 
     def run_loop(self):
         """Sequential per-system loop on the current stream."""
+        self._make_engines()
         for k in range(len(self.engines)):
             self._apply_one(k)
 
-    def capture(self):
+    def capture_engines_graph(self):
+        """Per-system engines as independent branches of one captured graph."""
         import torch
+        self._make_engines()
         main = torch.cuda.Stream()
         streams = [torch.cuda.Stream() for _ in self.engines]
         # warm every engine on its stream (plans and TMA descriptors exist before capture)
@@ -101,12 +125,14 @@ class SystemBatch:
         self.graph, self._streams, self._main = g, streams, main
         return g
 
-    def run(self):
+    def run_engines_graph(self):
         if self.graph is None:
-            self.capture()
+            self.capture_engines_graph()
         self.graph.replay()
 
     def close(self):
         self.graph = None
-        for e in self.engines:
-            e.close()
+        if self.engines:
+            for e in self.engines:
+                e.close()
+        self.batch.close()

@@ -94,16 +94,19 @@ def test_brownian_displacement_statistics(gpu_lib):
     assert relerr(cov, 2 * 0.5 * M) < 0.08  # 4000 samples: ~1/sqrt(4000) statistical error
 
 
-def test_uneven_batch_graph_matches_loop_and_oracle(gpu_lib, tmp_path, monkeypatch):
+def test_uneven_batch_matches_engines_and_oracle(gpu_lib):
+    """The native batch (one persistent launch per stage over all systems, one
+    cuFFT plan per distinct K, the step replayed as one CUDA graph) against the
+    per-system engines (loop and graph of engines) and the FP64 oracle, on two
+    interpolation tiles and every in-step concurrency mode."""
     import torch
     from spme_gb300.batch import SystemBatch, uneven_systems
-    monkeypatch.setenv("SPME_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     systems = uneven_systems(count=6, nmin=500, nmax=3000, seed=9)
     R = 4
     rng = np.random.default_rng(0)
     pos = [rng.uniform(0, s["L"], (s["N"], 3)) for s in systems]
     f = [rng.standard_normal((R, 3 * s["N"])) for s in systems]
-    b = SystemBatch(systems, nrhs=R)
+    b = SystemBatch(systems, nrhs=R, tune=False)
     pos_d = [torch.tensor(p, device="cuda") for p in pos]
     f_d = [torch.tensor(x, dtype=torch.float32, device="cuda") for x in f]
     u_d = [torch.zeros_like(x) for x in f_d]
@@ -113,15 +116,53 @@ def test_uneven_batch_graph_matches_loop_and_oracle(gpu_lib, tmp_path, monkeypat
     loop = [u.cpu().numpy().copy() for u in u_d]
     for u in u_d:
         u.zero_()
-    b.run()
-    b.run()  # replay twice
+    b.run_engines_graph()
     torch.cuda.synchronize()
-    for k, s in enumerate(systems):
-        got = u_d[k].cpu().numpy()
-        assert relerr(got, loop[k]) < 1e-6
-        ref = oracle.full(pos[k], s["L"], s["xi"], s["rc"], s["K"], s["p"], f[k], nthreads=4)
-        assert relerr(got, ref) < 1e-5
+    for k in range(len(systems)):
+        assert relerr(u_d[k].cpu().numpy(), loop[k]) < 1e-6
+    refs = [oracle.full(pos[k], s["L"], s["xi"], s["rc"], s["K"], s["p"],
+                        f[k].astype(np.float32).astype(np.float64), nthreads=4)
+            for k, s in enumerate(systems)]
+    for tile, overlap in (((8, 8, 8), 0), ((16, 8, 4), 3), ((16, 8, 4), 1), ((16, 8, 4), 2)):
+        b.batch.set_tile(*tile)
+        b.batch.set_overlap(overlap)
+        b.u_p.zero_()
+        b.run()
+        b.run()  # the captured graph replayed
+        b.batch.synchronize()
+        got = [x.cpu().numpy() for x in b.results()]
+        for k in range(len(systems)):
+            assert relerr(got[k], loop[k]) < 2e-6, (tile, overlap, k)
+            assert relerr(got[k], refs[k]) < 1e-5, (tile, overlap, k)
+    assert b.batch.launch_count() > 0
     b.close()
+
+
+def test_batch_apply_alpha_beta_fp64(gpu_lib):
+    """FP64 batch through set_positions + apply (no graph), u = beta u + alpha M f,
+    against the oracle at 1e-12; p = 4, 6, 8 and different K in one batch."""
+    import torch
+    systems = [dict(N=700, L=36.0, K=24, p=4, xi=0.35, rc=9.0, radius=1.0),
+               dict(N=1500, L=45.0, K=30, p=6, xi=0.3, rc=10.0, radius=1.2),
+               dict(N=900, L=40.0, K=32, p=8, xi=0.4, rc=8.0, radius=1.0)]
+    R = 2
+    rng = np.random.default_rng(4)
+    pos = [rng.uniform(0, s["L"], (s["N"], 3)) for s in systems]
+    f = [rng.standard_normal((R, 3 * s["N"])) for s in systems]
+    u0 = [rng.standard_normal((R, 3 * s["N"])) for s in systems]
+    bt = spme_gb300.Batch(systems, nrhs=R, precision="fp64")
+    pos_p = spme_gb300.Batch.pack([torch.tensor(p, device="cuda") for p in pos])
+    f_p = spme_gb300.Batch.pack([torch.tensor(x, device="cuda") for x in f])
+    u_p = spme_gb300.Batch.pack([torch.tensor(x, device="cuda") for x in u0])
+    bt.set_positions(pos_p)
+    bt.apply(f_p, u_p, alpha=0.7, beta=-0.3)
+    bt.synchronize()
+    got = [x.cpu().numpy() for x in bt.unpack(u_p)]
+    for k, s in enumerate(systems):
+        ref = oracle.full(pos[k], s["L"], s["xi"], s["rc"], s["K"], s["p"], f[k], alpha=0.7,
+                          beta=-0.3, u=u0[k], radius=s["radius"], nthreads=4)
+        assert relerr(got[k], ref) < 1e-12, k
+    bt.close()
 
 
 # (K, p, precision, nrhs): even / odd / 5-smooth K, Nyquist planes, R not a
