@@ -464,8 +464,16 @@ def run_gb300(args, w):
                                                             oref["real_self"])
             acc["oracle_rhs_checked"] = 2
             ers.close()
+        # the FP64 real-space sum timed alone (one more apply, stages serialized)
+        e64.set_profiling(2)
+        e64.set_positions(p64)
+        e64.apply(f64, u64)
+        torch.cuda.synchronize()
+        rs64_ms = e64.stage_times().get("realspace", 0.0)
+        e64.set_profiling(0)
         extra = {"fp64_plain": {"value": ns64, "unit": UNIT, "ms_per_apply": ms64,
-                                "terms": "recip+real+self", "nrhs": 1},
+                                "terms": "recip+real+self", "nrhs": 1,
+                                "realspace_ms": rs64_ms},
                  "fp32_batched_speedup_vs_fp64_plain": ns64 / value,
                  "accuracy": acc}
         e64.close()
@@ -489,6 +497,27 @@ def run_gb300(args, w):
             kern[k] = {"ms": stages[k]}
     for k, v in stages_serial.items():
         kern.setdefault(k, {})["ms_serialized"] = v
+    # real-space sum: arithmetic of the pair applications (9 FMA per pair and
+    # right-hand side: r.f, then F f + G r (r.f)) over the expected number of
+    # ordered pairs within rc, N (N - 1) (4/3) pi rc^3 / L^3, against the
+    # measured FMA peak (FP32 batched engine, FP64 plain path)
+    pairs = N * (N - 1) * (4.0 / 3.0) * np.pi * w["rc"] ** 3 / w["L"] ** 3
+    rs = {"pairs_expected": pairs, "flops_per_pair_rhs": 18}
+    try:
+        peak32, peak64 = spme_gb300.fma_peak("fp32"), spme_gb300.fma_peak("fp64")
+        rs.update({"fp32_fma_peak_tflops": peak32 / 1e12, "fp64_fma_peak_tflops": peak64 / 1e12})
+    except Exception:
+        peak32 = peak64 = None
+    t32 = stages_serial.get("realspace", 0.0)
+    if t32 > 0:
+        f32 = pairs * R * 18 / (t32 * 1e-3)
+        rs["fp32"] = {"ms": t32, "tflops": f32 / 1e12,
+                      "frac_of_measured_peak": f32 / peak32 if peak32 else None}
+    t64 = extra.get("fp64_plain", {}).get("realspace_ms", 0.0) if extra else 0.0
+    if t64 > 0:
+        f64 = pairs * 1 * 18 / (t64 * 1e-3)
+        rs["fp64"] = {"ms": t64, "nrhs": 1, "tflops": f64 / 1e12,
+                      "frac_of_measured_peak": f64 / peak64 if peak64 else None}
     dom = max(("spread", "influence", "interp"), key=lambda k: kern.get(k, {}).get("ms", 0.0))
     roof = None
     if dom in kern:
@@ -512,6 +541,7 @@ def run_gb300(args, w):
         "clocks": ck,
         "gpu_launches": launches,
         "kernels": kern,
+        "realspace_arithmetic": rs,
         "autotune": tune,
     }
     line.update(extra)

@@ -174,6 +174,12 @@ int spme_read_xyz(const char *path, int *np, double *box_size, double **pos, dou
 int spme_write_xyz(const char *path, int np, double box_size, const double *pos, double radius);
 void spme_free(void *p);
 
+/* Measured FMA throughput of the current device in FLOP/s (2 per FMA) for
+ * SPME_FP32 or SPME_FP64: independent FMA chains on every SM, timed with CUDA
+ * events.  The roofline denominator for the real-space sum's arithmetic.  No
+ * counterpart in the reference. */
+int spme_fma_peak(int precision, double *flops_per_s);
+
 /* ---- batches of independent systems --------------------------------------
  * No counterpart in the reference (its compute_spme, old-version/spme.c:560-726,
  * applies one system).  A batch holds systems of different size N_k, box L_k,

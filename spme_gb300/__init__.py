@@ -112,6 +112,7 @@ def load(path: str | None = None):
                               ctypes.POINTER(ctypes.POINTER(d)), ctypes.POINTER(ctypes.POINTER(d))]),
         "spme_write_xyz": (i, [ctypes.c_char_p, i, d, _P, d]),
         "spme_free": (None, [_P]),
+        "spme_fma_peak": (i, [i, ctypes.POINTER(d)]),
         "spme_batch_create": (i, [ctypes.POINTER(BatchSystem), i, i, i, ctypes.POINTER(_P)]),
         "spme_batch_destroy": (i, [_P]),
         "spme_batch_set_stream": (i, [_P, _P]),
@@ -200,6 +201,14 @@ def suggest_params(np_: int, box_size: float, radius: float = 1.0, tol: float = 
                                       float(rcut), ctypes.byref(out)), "spme_suggest_params")
     return {"np": out.np, "box_size": out.box_size, "xi": out.xi, "dim": out.dim,
             "porder": out.porder, "radius": out.radius, "rcut": out.rcut}
+
+
+def fma_peak(precision: str = "fp32") -> float:
+    """Measured FMA throughput of the current device in FLOP/s."""
+    out = ctypes.c_double()
+    _check(load().spme_fma_peak(SPME_FP32 if precision == "fp32" else SPME_FP64,
+                                ctypes.byref(out)), "spme_fma_peak")
+    return out.value
 
 
 def next_smooth(n: int) -> int:
