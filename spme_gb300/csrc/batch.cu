@@ -96,33 +96,46 @@ __global__ void k_batch_keys(const double *__restrict__ pos, int n, const int *_
 // record stride ws for the whole batch).
 template <typename T, int P>
 __device__ __forceinline__ void batch_record(const T *__restrict__ pfrac, int i, int ws, T *out) {
-    T w[3][P];
+    T w[P];
 #pragma unroll
-    for (int d = 0; d < 3; d++) bspline_weights<T, P>(pfrac[3 * i + d], w[d]);
+    for (int d = 0; d < 3; d++) {
+        bspline_weights<T, P>(pfrac[3 * i + d], w);
 #pragma unroll
-    for (int d = 0; d < 3; d++)
-#pragma unroll
-        for (int j = 0; j < P; j++) out[d * P + j] = w[d][j];
+        for (int j = 0; j < P; j++) out[d * P + j] = w[j];
+    }
     for (int j = 3 * P; j < ws; j++) out[j] = T(0);
 }
 
+// (records assembled in shared memory, written as one contiguous run)
+constexpr int kRecThreads = 128;
+constexpr int kMaxWs = 24;  // record stride of order 8
+
 template <typename T>
-__global__ void k_batch_records(const uint32_t *__restrict__ pstart, const T *__restrict__ pfrac,
-                                const int *__restrict__ perm, int n,
-                                const int *__restrict__ sysid, const BatchGeo *__restrict__ geo,
-                                int ws, int *__restrict__ rec_idx, uint32_t *__restrict__ rec_start,
-                                T *__restrict__ rec_w) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const int i = perm[s];
-    rec_idx[s] = i;
-    rec_start[s] = pstart[i];
-    T *out = rec_w + (size_t)s * ws;
-    switch (geo[sysid[i]].g.p) {
-        case 4: batch_record<T, 4>(pfrac, i, ws, out); break;
-        case 6: batch_record<T, 6>(pfrac, i, ws, out); break;
-        default: batch_record<T, 8>(pfrac, i, ws, out); break;
+__global__ void __launch_bounds__(kRecThreads)
+k_batch_records(const uint32_t *__restrict__ pstart, const T *__restrict__ pfrac,
+                const int *__restrict__ perm, int n, const int *__restrict__ sysid,
+                const BatchGeo *__restrict__ geo, int ws, int *__restrict__ rec_idx,
+                uint32_t *__restrict__ rec_start, T *__restrict__ rec_w) {
+    __shared__ __align__(16) T sm[kRecThreads * kMaxWs];
+    const int s0 = blockIdx.x * kRecThreads;
+    const int s = s0 + threadIdx.x;
+    if (s < n) {
+        const int i = perm[s];
+        rec_idx[s] = i;
+        rec_start[s] = pstart[i];
+        T *out = sm + (size_t)threadIdx.x * ws;
+        switch (geo[sysid[i]].g.p) {
+            case 4: batch_record<T, 4>(pfrac, i, ws, out); break;
+            case 6: batch_record<T, 6>(pfrac, i, ws, out); break;
+            default: batch_record<T, 8>(pfrac, i, ws, out); break;
+        }
     }
+    __syncthreads();
+    const int cnt = min(kRecThreads, n - s0);
+    const int vq = ws * (int)sizeof(T) / 16;
+    float4 *dst = reinterpret_cast<float4 *>(rec_w + (size_t)s0 * ws);
+    const float4 *src = reinterpret_cast<const float4 *>(sm);
+    for (int v = threadIdx.x; v < cnt * vq; v += kRecThreads) dst[v] = src[v];
 }
 
 // Caller layout (system k at element 3 R P_k, rows of 3 N_k) <-> packed rows
@@ -720,10 +733,10 @@ int positions_body(_spme_batch_t *b, const double *pos) {
     launch_scatter(b->d_key2, b->d_slot2, b->d_off2, n, b->d_perm2, s);
     launch_scan(b->d_cnt3, b->ncell_keys, b->d_off3, b->d_scan_tmp, s);
     launch_scatter(b->d_key3, b->d_slot3, b->d_off3, n, b->d_perm3, s);
-    k_batch_records<T><<<nblk(n, 128), 128, 0, s>>>(b->d_pstart, (const T *)b->d_pfrac,
+    k_batch_records<T><<<nblk(n, kRecThreads), kRecThreads, 0, s>>>(b->d_pstart, (const T *)b->d_pfrac,
                                                     b->d_perm1, n, b->d_sysid, b->d_geo, b->ws,
                                                     b->d_ridx1, b->d_rst1, (T *)b->d_rw1);
-    k_batch_records<T><<<nblk(n, 128), 128, 0, s>>>(b->d_pstart, (const T *)b->d_pfrac,
+    k_batch_records<T><<<nblk(n, kRecThreads), kRecThreads, 0, s>>>(b->d_pstart, (const T *)b->d_pfrac,
                                                     b->d_perm2, n, b->d_sysid, b->d_geo, b->ws,
                                                     b->d_ridx2, b->d_rst2, (T *)b->d_rw2);
     launch_cell_gather(b->d_prel, b->d_perm3, n, sizeof(T) == 4, b->d_cpos, s);

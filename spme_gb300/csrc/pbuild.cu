@@ -190,26 +190,44 @@ __global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ s
     perm[off[key[i]] + slot[i]] = i;
 }
 
+// The block's records are assembled in shared memory and written as one
+// contiguous run of 16-byte stores: a record is WS elements (80 bytes at p = 6
+// FP32), and per-thread record stores would touch a separate sector per lane.
+constexpr int kRecThreads = 128;
+
 template <typename T, int P>
-__global__ void k_records(const uint32_t *__restrict__ pstart, const T *__restrict__ pfrac,
-                          const int *__restrict__ perm, int n, int *__restrict__ rec_idx,
-                          uint32_t *__restrict__ rec_start, T *__restrict__ rec_w) {
+__global__ void __launch_bounds__(kRecThreads)
+k_records(const uint32_t *__restrict__ pstart, const T *__restrict__ pfrac,
+          const int *__restrict__ perm, int n, int *__restrict__ rec_idx,
+          uint32_t *__restrict__ rec_start, T *__restrict__ rec_w) {
     constexpr int WS = RecordWidth<T, P>::value;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    int i = perm[s];
-    T w[3][P];
+    constexpr int VQ = WS * (int)sizeof(T) / 16;  // 16-byte pieces per record
+    __shared__ __align__(16) T sm[kRecThreads * WS];
+    const int s0 = blockIdx.x * kRecThreads;
+    const int s = s0 + threadIdx.x;
+    if (s < n) {
+        const int i = perm[s];
+        T row[WS];
+        T w[P];
 #pragma unroll
-    for (int d = 0; d < 3; d++) bspline_weights<T, P>(pfrac[3 * i + d], w[d]);
-    rec_idx[s] = i;
-    rec_start[s] = pstart[i];
-    T *out = rec_w + (size_t)s * WS;
+        for (int d = 0; d < 3; d++) {
+            bspline_weights<T, P>(pfrac[3 * i + d], w);
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+            for (int j = 0; j < P; j++) row[d * P + j] = w[j];
+        }
 #pragma unroll
-        for (int j = 0; j < P; j++) out[d * P + j] = w[d][j];
+        for (int j = 3 * P; j < WS; j++) row[j] = T(0);
+        rec_idx[s] = i;
+        rec_start[s] = pstart[i];
+        float4 *dst = reinterpret_cast<float4 *>(sm + (size_t)threadIdx.x * WS);
 #pragma unroll
-    for (int j = 3 * P; j < WS; j++) out[j] = T(0);
+        for (int q = 0; q < VQ; q++) dst[q] = reinterpret_cast<const float4 *>(row)[q];
+    }
+    __syncthreads();
+    const int cnt = min(kRecThreads, n - s0);
+    float4 *out = reinterpret_cast<float4 *>(rec_w + (size_t)s0 * WS);
+    const float4 *src = reinterpret_cast<const float4 *>(sm);
+    for (int v = threadIdx.x; v < cnt * VQ; v += kRecThreads) out[v] = src[v];
 }
 
 // Cell-relative positions in cell order, gathered from the keys pass's output.
@@ -297,10 +315,11 @@ template <typename T>
 void launch_records(const uint32_t *pstart, const T *pfrac, const int *perm, int n, int p,
                     int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s) {
     if (n <= 0) return;
+    const int nb = nblk(n, kRecThreads);
     switch (p) {
-        case 4: k_records<T, 4><<<nblk(n, 128), 128, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
-        case 6: k_records<T, 6><<<nblk(n, 128), 128, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
-        case 8: k_records<T, 8><<<nblk(n, 128), 128, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
+        case 4: k_records<T, 4><<<nb, kRecThreads, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
+        case 6: k_records<T, 6><<<nb, kRecThreads, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
+        case 8: k_records<T, 8><<<nb, kRecThreads, 0, s>>>(pstart, pfrac, perm, n, rec_idx, rec_start, rec_w); break;
         default: break;
     }
 }
