@@ -16,14 +16,15 @@
 //   * the warp walks the p (p + 1) start columns that reach its column pair and
 //     their z runs, so every particle it visits covers at least one of its two
 //     columns (a half whose column is missed multiplies by a zero weight);
-//   * visits are staged 32 at a time (one lane per visit: record, weights of
+//   * visits are staged in batches (one lane per visit: record, weights of
 //     both columns, force-row offset) and ranked by their z offset relative to
 //     the tile (a 5-bit radix rank from ballots), so the accumulation walks the
 //     offsets in a compile-time sequence, each with straight-line code for its
-//     planes: no per-visit dispatch;
+//     planes (FP32: one body per pair of offsets): no per-visit dispatch;
 //   * FP32 accumulators are pairs of planes, updated with the packed
 //     two-lane FMA (fma.rn.f32x2, sm_100 and later): a visit whose first plane
-//     is odd uses weights staged one plane later (0, w_0 .. w_{p-1}, 0);
+//     is odd uses weights staged one plane later (0, w_0 .. w_{p-1}, 0), one
+//     whose first plane is even (w_0 .. w_{p-1}, 0, 0);
 //   * force rows are read as one vector per lane: the rows are gathered per
 //     pass into a padded layout where each lane's CPL components are
 //     contiguous (spread_cols_row_width);
@@ -111,20 +112,18 @@ struct WRow {
     static constexpr int value = (raw + per16 - 1) / per16 * per16;
 };
 
-// FP32: acc[m][k] holds planes (2m, 2m+1) of component k; a visit whose first
-// plane is D adds (w[2i], w[2i+1]) f_k to the pairs m = floor(D/2) + i that lie
-// inside [0, TZ/2) (w staged shifted by one plane for odd D).
-template <int P, int CPL, int TZ, int D, int NW>
-__device__ __forceinline__ void add_pairs(float2 (&acc)[TZ / 2][CPL], const float (&w)[NW],
-                                          const float (&f)[CPL]) {
-    constexpr int ODD = D & 1;
-    constexpr int M0 = (D - ODD) / 2;
-    constexpr int NPAIR = P / 2 + ODD;
+// FP32, one body for the offsets 2 M0 and 2 M0 + 1: P/2 + 1 pairs from pair M0
+// (the staged weights put an odd offset's planes one slot later; an even
+// offset's last pair is zero).
+template <int P, int CPL, int TZ, int M0, int NW>
+__device__ __forceinline__ void add_pair_run(float2 (&acc)[TZ / 2][CPL], const float (&w)[NW],
+                                             const float (&f)[CPL]) {
+    static_assert(NW >= P + 2, "staged row holds P + 2 weights");
     float2 fd[CPL];
 #pragma unroll
     for (int k = 0; k < CPL; k++) fd[k] = make_float2(f[k], f[k]);
 #pragma unroll
-    for (int i = 0; i < NPAIR; i++) {
+    for (int i = 0; i < P / 2 + 1; i++) {
         const int m = M0 + i;
         if (m >= 0 && m < TZ / 2) {
             const float2 wp = make_float2(w[2 * i], w[2 * i + 1]);
@@ -364,28 +363,47 @@ __device__ __forceinline__ void spread_cols_body(const SpreadColsArgs<T> &A, int
             cp_async_wait_all();
             __syncwarp();
             // accumulate in offset order
-            int j = 0;
-            static_for<ND>([&](auto bc) {
-                constexpr int D = decltype(bc)::value - (P - 1);  // the bucket's z offset
-                const int cnt = __popc(__ballot_sync(0xffffffffu, dl == D + (P - 1)));
-                for (int k = 0; k < cnt; k++, j++) {
-                    T f[CPL];
-                    if constexpr (CPL > 1) {
-                        T fv[PC];
-                        load_vec<T, PC>(fst + j * LR + l16 * PC, fv);
+            auto visit_force = [&](int j, T (&f)[CPL]) {
+                if constexpr (CPL > 1) {
+                    T fv[PC];
+                    load_vec<T, PC>(fst + j * LR + l16 * PC, fv);
 #pragma unroll
-                        for (int c = 0; c < CPL; c++) f[c] = fv[c];
-                    } else {
-                        f[0] = lane_live ? fst[j * LR + l16] : T(0);
-                    }
-                    T wt[WR];
-                    load_vec<T, WR>(&ws.wt[j][half][0], wt);
-                    if constexpr (F32)
-                        add_pairs<P, CPL, TZ, D, WR>(acc, wt, f);
-                    else
-                        add_planes<P, CPL, TZ, D, WR>(acc, wt, f);
+                    for (int c = 0; c < CPL; c++) f[c] = fv[c];
+                } else {
+                    f[0] = lane_live ? fst[j * LR + l16] : T(0);
                 }
-            });
+            };
+            int j = 0;
+            if constexpr (F32) {
+                // FP32: one bucket per first plane pair m0 = floor(offset / 2) (the
+                // offsets 2 m0 and 2 m0 + 1 share one straight-line body of P/2 + 1
+                // pairs; an even offset's last pair has zero weights)
+                constexpr int NDP = TZ / 2 + P / 2;
+                const int bl = (dl + 1) >> 1;  // m0 + P/2 (31: none)
+                static_for<NDP>([&](auto bc) {
+                    constexpr int M0 = decltype(bc)::value - P / 2;
+                    const int cnt = __popc(__ballot_sync(0xffffffffu, bl == M0 + P / 2));
+                    for (int k = 0; k < cnt; k++, j++) {
+                        T f[CPL];
+                        visit_force(j, f);
+                        T wt[WR];
+                        load_vec<T, WR>(&ws.wt[j][half][0], wt);
+                        add_pair_run<P, CPL, TZ, M0, WR>(acc, wt, f);
+                    }
+                });
+            } else {
+                static_for<ND>([&](auto bc) {
+                    constexpr int D = decltype(bc)::value - (P - 1);  // the bucket's z offset
+                    const int cnt = __popc(__ballot_sync(0xffffffffu, dl == D + (P - 1)));
+                    for (int k = 0; k < cnt; k++, j++) {
+                        T f[CPL];
+                        visit_force(j, f);
+                        T wt[WR];
+                        load_vec<T, WR>(&ws.wt[j][half][0], wt);
+                        add_planes<P, CPL, TZ, D, WR>(acc, wt, f);
+                    }
+                });
+            }
             __syncwarp();
         }
     }
