@@ -548,10 +548,34 @@ def run_gb300(args, w):
         "autotune": tune,
     }
     line.update(extra)
+    if ws == 1 and args.workload == "large" and not args.no_secondary:
+        line["secondary_workloads"] = run_secondary(args)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def run_secondary(args):
+    """The single-right-hand-side system, the mid-size 16-right-hand-side system
+    and the uneven batch, each in a child process (its own engines and memory),
+    summarised in the main line."""
+    out = {}
+    for wl in ("scale_up", "multi_rhs", "uneven_batch"):
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", wl, "--steps",
+               str(max(5, args.steps)), "--warmup", "3", "--no-cpu-baseline", "--no-secondary"]
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+            d = json.loads([x for x in r.stdout.splitlines() if x.startswith("{")][-1])
+        except Exception as exc:  # reported, never fatal for the main line
+            out[wl] = {"error": str(exc)[:200]}
+            continue
+        keep = ("value", "unit", "ms_per_step", "config", "e2e", "kernels", "per_system_loop",
+                "engines_graph", "speedup_vs_loop", "speedup_vs_engines_graph",
+                "stages_ms_serialized", "gpu_launches", "autotune", "fp64_plain",
+                "fp32_batched_speedup_vs_fp64_plain", "accuracy", "clocks")
+        out[wl] = {k: d[k] for k in keep if k in d}
+    return out
 
 
 def run_batch(args, w):
@@ -645,6 +669,8 @@ def main():
     ap.add_argument("--no-oracle-check", action="store_true",
                     help="skip the FP64 oracle check of the timed result (outside the timed region)")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the mid-size and uneven-batch workloads after the large one")
     ap.add_argument("--tile", default=None,
                     help="fixed mesh tile 'tx,ty,tz' instead of autotuning (e.g. for profiling)")
     args = ap.parse_args()
