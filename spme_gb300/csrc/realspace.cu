@@ -203,8 +203,13 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     const PairTable &tab = A.tab;
     __shared__ int nb_beg[27], nb_pre[28], nnb;
     __shared__ G nb_shift[27][3];
-    __shared__ G cx[kCap], cy[kCap], cz[kCap];
-    __shared__ int cj[kCap];
+    // a staged candidate: position in the CTA cell's frame and particle id in
+    // one 16-byte (FP32) or 32-byte (FP64) record
+    struct __align__(4 * sizeof(G)) Cand {
+        G x, y, z;
+        int j;
+    };
+    __shared__ Cand cand[kCap];
     // FP64 engines: FP32 copies for a conservative first distance test (the FP64
     // test then runs only on candidates that pass it)
     constexpr bool kPre = sizeof(G) == 8;
@@ -221,42 +226,63 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int C = 3 * R;
-    if (tid == 0) {
+    // neighbour table: lane k of warp 0 takes neighbour cell k (27 of them, or
+    // the cell alone when nc < 3), candidate offsets by a warp scan
+    if (warp == 0) {
         const int ccx = cell % nc, ccy = (cell / nc) % nc, ccz = cell / (nc * nc);
-        const int span = nc >= 3 ? 1 : 0;
-        int k = 0, pre = 0;
-        for (int dz = -span; dz <= span; dz++)
-            for (int dy = -span; dy <= span; dy++)
-                for (int dx = -span; dx <= span; dx++) {
-                    int c2 = (pmod(ccz + dz, nc) * nc + pmod(ccy + dy, nc)) * nc + pmod(ccx + dx, nc);
-                    nb_beg[k] = cell_off[c2];
-                    nb_pre[k] = pre;
-                    nb_shift[k][0] = (G)dx * h;
-                    nb_shift[k][1] = (G)dy * h;
-                    nb_shift[k][2] = (G)dz * h;
-                    pre += cell_off[c2 + 1] - cell_off[c2];
-                    k++;
-                }
-        nb_pre[k] = pre;
-        nnb = k;
+        const int nk = nc >= 3 ? 27 : 1;
+        int cnt = 0;
+        if (lane < nk) {
+            const int dx = nk == 1 ? 0 : lane % 3 - 1, dy = nk == 1 ? 0 : (lane / 3) % 3 - 1,
+                      dz = nk == 1 ? 0 : lane / 9 - 1;
+            auto wrap = [nc](int v) { return v < 0 ? v + nc : (v >= nc ? v - nc : v); };
+            const int c2 = (wrap(ccz + dz) * nc + wrap(ccy + dy)) * nc + wrap(ccx + dx);
+            const int b = __ldg(cell_off + c2);
+            cnt = __ldg(cell_off + c2 + 1) - b;
+            nb_beg[lane] = b;
+            nb_shift[lane][0] = (G)dx * h;
+            nb_shift[lane][1] = (G)dy * h;
+            nb_shift[lane][2] = (G)dz * h;
+        }
+        int inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane < nk) nb_pre[lane] = inc - cnt;
+        if (lane == nk - 1) {
+            nb_pre[nk] = inc;
+            nnb = nk;
+        }
     }
     __syncthreads();
     const int ncand = nb_pre[nnb];
     const bool staged = ncand <= kCap;
+    // neighbour k holding candidate q: nb_pre[k] <= q < nb_pre[k + 1]
+    auto find_nb = [&](int q) {
+        int lo = 0, hi = nnb;
+        while (hi - lo > 1) {
+            const int m = (lo + hi) >> 1;
+            if (nb_pre[m] <= q) lo = m; else hi = m;
+        }
+        return lo;
+    };
     if (staged) {
         for (int q = tid; q < ncand; q += kThreads) {
-            int k = 0;
-            while (q >= nb_pre[k + 1]) k++;
+            const int k = find_nb(q);
             const int js = nb_beg[k] + (q - nb_pre[k]);
             const auto p = cpos[js];
-            cx[q] = p.x + nb_shift[k][0];
-            cy[q] = p.y + nb_shift[k][1];
-            cz[q] = p.z + nb_shift[k][2];
-            cj[q] = cell_perm[js];
+            Cand c;
+            c.x = p.x + nb_shift[k][0];
+            c.y = p.y + nb_shift[k][1];
+            c.z = p.z + nb_shift[k][2];
+            c.j = cell_perm[js];
+            cand[q] = c;
             if constexpr (kPre) {
-                fx[q] = (float)cx[q];
-                fy[q] = (float)cy[q];
-                fz[q] = (float)cz[q];
+                fx[q] = (float)c.x;
+                fy[q] = (float)c.y;
+                fz[q] = (float)c.z;
             }
         }
     }
@@ -272,13 +298,13 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     // candidate q -> position in this cell's frame and particle id
     auto candidate = [&](int q, G &x, G &y, G &z, int &j) {
         if (staged) {
-            x = cx[q];
-            y = cy[q];
-            z = cz[q];
-            j = cj[q];
+            const Cand c = cand[q];
+            x = c.x;
+            y = c.y;
+            z = c.z;
+            j = c.j;
         } else {
-            int k = 0;
-            while (q >= nb_pre[k + 1]) k++;
+            const int k = find_nb(q);
             const int js = nb_beg[k] + (q - nb_pre[k]);
             const auto p = cpos[js];
             x = p.x + nb_shift[k][0];
