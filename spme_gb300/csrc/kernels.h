@@ -203,6 +203,16 @@ template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
                              const T *F, int R, double L, double rc, double xi, double a,
                              int with_self, const PairTable &tab, T *W, cudaStream_t s);
+// FP32 pair-function coefficients of one (xi, a) and the FP32 copies of the
+// geometry (real_args fills them): far field (r >= 2a), with ir = 1/r,
+//   F = erfc(xi r) (0.75 ir + c1 ir^3) + e^{-xi^2 r^2} (A4 r^4 + A2 r^2 + A0 + Am2 ir^2)
+//   G = erfc(xi r) (0.75 ir + c3 ir^3) + e^{-xi^2 r^2} (-A4 r^4 + B2 r^2 + B0 + Bm2 ir^2)
+// near field: xi, xi3a2 = xi^3 a^2, ia = 1/a, n1 = 9/(32 a^2), n2 = 3/(32 a^2).
+struct RealCoef {
+    float xi, xi2, a2x4, xi3a2, ia, n1, n2;
+    float A4, A2, A0, Am2, B2, B0, Bm2, c1, c3;
+    float L, h, rc2, self_c;
+};
 // Arguments of one system's real-space sum (cell_off indexed by this system's
 // cells; slots, positions and rows global).
 template <typename T>
@@ -215,6 +225,7 @@ struct RealArgs {
     int nc, R, with_self;
     double L, h, rc2, xi, a, self_c;
     PairTable tab;
+    RealCoef cf;
 };
 double real_self_coeff(double xi, double a);
 template <typename T>

@@ -20,12 +20,9 @@ namespace {
 
 constexpr int kThreads = 64;  // two warps per cell: ~4-5 particles each at typical densities
 
-__device__ __forceinline__ float d_erfc(float x) { return erfcf(x); }
 __device__ __forceinline__ double d_erfc(double x) { return erfc(x); }
-__device__ __forceinline__ float d_exp(float x) { return expf(x); }
 __device__ __forceinline__ double d_exp(double x) { return exp(x); }
 
-__device__ __forceinline__ float d_erf(float x) { return erff(x); }
 __device__ __forceinline__ double d_erf(double x) { return erf(x); }
 
 // Maclaurin coefficients (without the 2/sqrt(pi) factor) of S(x) = erf(x)/x,
@@ -89,6 +86,54 @@ __device__ __forceinline__ void real_FG(T r, T xi, T a, T &F, T &G) {
                            T(1.5) * xi * a - T(2) * xi3 * a3 - T(3) * xi * a3 * ir2);
     F = f / a;
     G = g / a;
+}
+
+// FP32 engines: F, G and ir = 1/r (0 at r = 0) from r^2, with the launch's
+// coefficients (RealCoef): one reciprocal square root gives r, 1/r and the
+// unit vector; the far field (r >= 2a) is real_FG's far form divided through
+// by a, the near field real_FG's cancellation-free form with FP32 constants.
+__device__ __forceinline__ void real_FG_f32(float r2, const RealCoef &c, float &F, float &G,
+                                            float &ir) {
+    constexpr float rsp = 0.56418958354775628695f;  // 1/sqrt(pi)
+    ir = r2 > 0.f ? rsqrtf(r2) : 0.f;
+    const float r = r2 * ir;
+    if (r2 < c.a2x4) {
+        const float x = c.xi * r, x2 = x * x, e = expf(-x2);
+        float S, P;
+        if (x < 0.5f) {
+            constexpr float ks[10] = {1.0f, -1.0f / 3, 1.0f / 10, -1.0f / 42, 1.0f / 216,
+                                      -1.0f / 1320, 1.0f / 9360, -1.0f / 75600,
+                                      1.0f / 685440, -1.0f / 6894720};
+            constexpr float kp[10] = {2.0f / 3, -2.0f / 5, 1.0f / 7, -1.0f / 27, 1.0f / 132,
+                                      -1.0f / 780, 1.0f / 5400, -1.0f / 42840,
+                                      1.0f / 383040, -1.0f / 3810240};
+            S = 0.f;
+            P = 0.f;
+#pragma unroll
+            for (int k = 9; k >= 0; k--) {
+                S = fmaf(S, x2, ks[k]);
+                P = fmaf(P, x2, kp[k]);
+            }
+            S *= 2.f * rsp;
+            P *= 2.f * rsp;
+        } else {
+            const float ef = erff(x), ix = 1.f / x;
+            S = ef * ix;
+            P = (ef - 2.f * rsp * x * e) * (ix * ix * ix);
+        }
+        const float x4 = x2 * x2, re = rsp * e;
+        F = c.xi * (-0.75f * S + re * (3.f * x2 - 4.5f)) +
+            c.xi3a2 * (-0.5f * P + re * (4.f * x4 - 20.f * x2 + 14.f)) + (c.ia - c.n1 * r);
+        G = c.xi * (-0.75f * S + re * (1.5f - 3.f * x2)) +
+            c.xi3a2 * (1.5f * P + re * (-4.f * x4 + 16.f * x2 - 2.f)) + c.n2 * r;
+        return;
+    }
+    const float ec = erfcf(c.xi * r), e = expf(-c.xi2 * r2);
+    const float ir2 = ir * ir, ir3 = ir2 * ir, r4 = r2 * r2;
+    const float pF = fmaf(c.A4, r4, fmaf(c.A2, r2, fmaf(c.Am2, ir2, c.A0)));
+    const float pG = fmaf(-c.A4, r4, fmaf(c.B2, r2, fmaf(c.Bm2, ir2, c.B0)));
+    F = ec * fmaf(c.c1, ir3, 0.75f * ir) + e * pF;
+    G = ec * fmaf(c.c3, ir3, 0.75f * ir) + e * pG;
 }
 
 // F and G from the per-engine Chebyshev table (FP64 engines): false when r is
@@ -198,8 +243,12 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     const T *__restrict__ F = A.F;
     T *__restrict__ W = A.W;
     const int R = A.R, with_self = A.with_self;
-    const G L = (G)A.L, h = (G)A.h, rc2 = (G)A.rc2;
-    const T xi = (T)A.xi, a = (T)A.a, self_c = (T)A.self_c;
+    constexpr bool kF32 = sizeof(T) == 4;
+    // FP32: the geometry and coefficients as FP32 copies (no conversions here)
+    const G L = kF32 ? (G)A.cf.L : (G)A.L, h = kF32 ? (G)A.cf.h : (G)A.h,
+            rc2 = kF32 ? (G)A.cf.rc2 : (G)A.rc2;
+    const T xi = kF32 ? (T)A.cf.xi : (T)A.xi, a = (T)A.a;
+    const T self_c = kF32 ? (T)A.cf.self_c : (T)A.self_c;
     const PairTable &tab = A.tab;
     __shared__ int nb_beg[27], nb_pre[28], nnb;
     __shared__ G nb_shift[27][3];
@@ -220,7 +269,7 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     struct __align__(16) PairRec {
         typename Geo4<T>::type rf;  // (rhat_x, rhat_y, rhat_z, F)
         const T *frow;
-        T G;
+        T gfac;
     };
     __shared__ PairRec prec[kWarps][32];
 
@@ -291,7 +340,8 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     // the FP32 test accepts a superset of the pairs within rc: coordinates lie
     // within 3 cells, so FP32 rounding moves d^2 by far less than the margin
     const bool pre = kPre && staged && !single;
-    const float pre_r2 = (float)((double)rc2 * 1.0001 + 1e-5 * 9.0 * (double)h * (double)h);
+    const float pre_r2 =
+        kPre ? (float)((double)rc2 * 1.0001 + 1e-5 * 9.0 * (double)h * (double)h) : 0.f;
     const G invL = G(1) / L;
     const int ib0 = cell_off[cell], ie = cell_off[cell + 1];
 
@@ -338,24 +388,27 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
                         d1 -= L * d_rint(d1 * invL);
                         d2 -= L * d_rint(d2 * invL);
                     }
-                    const G rr = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
                     T Fv, Gv;
-                    bool done = false;
-                    if constexpr (sizeof(T) == 8) {
+                    G ir;  // coincident particles (r = 0): no direction, the G term vanishes
+                    if constexpr (kF32) {
+                        real_FG_f32(d0 * d0 + d1 * d1 + d2 * d2, A.cf, Fv, Gv, ir);
+                    } else {
+                        const G rr = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
                         double Fd, Gd;
-                        done = table_FG(tab, (double)rr, Fd, Gd);
-                        Fv = (T)Fd;
-                        Gv = (T)Gd;
+                        if (table_FG(tab, (double)rr, Fd, Gd)) {
+                            Fv = (T)Fd;
+                            Gv = (T)Gd;
+                        } else {
+                            real_FG<T>((T)rr, xi, a, Fv, Gv);
+                        }
+                        ir = rr > G(0) ? G(1) / rr : G(0);
                     }
-                    if (!done) real_FG<T>((T)rr, xi, a, Fv, Gv);
-                    // coincident particles (r = 0): no direction, the G term vanishes
-                    const G ir = rr > G(0) ? G(1) / rr : G(0);
                     PairRec &pq = prec[warp][lane];
                     pq.rf.x = (T)(d0 * ir);
                     pq.rf.y = (T)(d1 * ir);
                     pq.rf.z = (T)(d2 * ir);
                     pq.rf.w = Fv;
-                    pq.G = Gv;
+                    pq.gfac = Gv;
                     pq.frow = F + (size_t)j * C;
                 }
                 __syncwarp();
@@ -368,7 +421,7 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
                         const T *fj = pq.frow + 3 * r;
                         const T f0 = __ldg(fj), f1 = __ldg(fj + 1), f2 = __ldg(fj + 2);
                         const T rx = rf.x, ry = rf.y, rz = rf.z;
-                        const T Fk = rf.w, Gd = pq.G * (rx * f0 + ry * f1 + rz * f2);
+                        const T Fk = rf.w, Gd = pq.gfac * (rx * f0 + ry * f1 + rz * f2);
                         s0 += Fk * f0 + Gd * rx;
                         s1 += Fk * f1 + Gd * ry;
                         s2 += Fk * f2 + Gd * rz;
@@ -455,8 +508,7 @@ k_realspace_batch(const RealArgs<T> *__restrict__ sys, const int *__restrict__ p
                   int total) {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int k = batch_find(prefix, nsys, w);
-        const RealArgs<T> A = sys[k];
-        realspace_body<T, G>(A, w - prefix[k]);
+        realspace_body<T, G>(sys[k], w - prefix[k]);
         __syncthreads();
     }
 }
@@ -488,6 +540,29 @@ RealArgs<T> real_args(int nc, const int *cell_off, const int *cell_perm, const v
     A.a = a;
     A.self_c = real_self_coeff(xi, a);
     A.tab = tab;
+    const double rsp = 0.56418958354775628695, a2 = a * a, xi2 = xi * xi, xi3 = xi2 * xi,
+                 xi5 = xi3 * xi2, xi7 = xi5 * xi2;
+    RealCoef &c = A.cf;
+    c.xi = (float)xi;
+    c.xi2 = (float)xi2;
+    c.a2x4 = (float)(4.0 * a2);
+    c.xi3a2 = (float)(xi3 * a2);
+    c.ia = (float)(1.0 / a);
+    c.n1 = (float)(9.0 / (32.0 * a2));
+    c.n2 = (float)(3.0 / (32.0 * a2));
+    c.A4 = (float)(4.0 * rsp * xi7 * a2);
+    c.A2 = (float)(rsp * (3.0 * xi3 - 20.0 * xi5 * a2));
+    c.A0 = (float)(rsp * (-4.5 * xi + 14.0 * xi3 * a2));
+    c.Am2 = (float)(rsp * xi * a2);
+    c.B2 = (float)(rsp * (-3.0 * xi3 + 16.0 * xi5 * a2));
+    c.B0 = (float)(rsp * (1.5 * xi - 2.0 * xi3 * a2));
+    c.Bm2 = (float)(-3.0 * rsp * xi * a2);
+    c.c1 = (float)(0.5 * a2);
+    c.c3 = (float)(-1.5 * a2);
+    c.L = (float)L;
+    c.h = (float)A.h;
+    c.rc2 = (float)A.rc2;
+    c.self_c = (float)A.self_c;
     return A;
 }
 
