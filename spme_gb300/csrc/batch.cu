@@ -44,7 +44,7 @@ struct BatchGeo {
 
 template <typename T> struct V4T;
 template <> struct V4T<float> { using type = float4; };
-template <> struct V4T<double> { using type = double4; };
+template <> struct V4T<double> { using type = double4_32a; };
 
 // Sort keys (with slots from atomic counts), stencil starts, fractional mesh
 // coordinates and cell-relative positions of every particle of every system

@@ -141,7 +141,7 @@ struct _spme_t {
     void *d_srec_w = nullptr;
     void *d_Fs = nullptr;  // force rows in start-cell order
     int *d_ccount = nullptr, *d_coff = nullptr, *d_cperm = nullptr;
-    void *d_cpos = nullptr;  // float4 (FP32 engine) or double4 (FP64 engine)
+    void *d_cpos = nullptr;  // float4 (FP32 engine) or double4_32a (FP64 engine)
     void *d_prel = nullptr;  // the same in particle order (from the keys pass)
     void *d_pair = nullptr;  // Chebyshev table of the pair functions (FP64 engines)
     spme::PairTable pair;
@@ -504,8 +504,8 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_ccount, sizeof(int) * ncell));
         TRY(dalloc(&e->d_coff, sizeof(int) * (ncell + 1)));
         TRY(dalloc(&e->d_cperm, sizeof(int) * n));
-        TRY(dalloc(&e->d_cpos, sizeof(double4) * n));
-        TRY(dalloc(&e->d_prel, sizeof(double4) * n));
+        TRY(dalloc(&e->d_cpos, sizeof(double4_32a) * n));
+        TRY(dalloc(&e->d_prel, sizeof(double4_32a) * n));
         // FP64: the pair functions from a Chebyshev table instead of erfc / exp
         std::vector<double> coef;
         if (!is_fp32(e) && spme::build_pair_table(prm.xi, prm.radius, prm.rcut, &coef, &e->pair)) {

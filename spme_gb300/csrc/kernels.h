@@ -19,12 +19,12 @@ namespace spme {
 // the positions.  A null count skips that key.  With a mesh key, pstart (n)
 // and pfrac (3n values of the engine's type: float when fp32) receive each
 // particle's packed stencil start and fractional mesh coordinates; with the
-// cell key, prel (n float4 / double4) its position relative to its cell.
+// cell key, prel (n float4 / double4_32a) its position relative to its cell.
 void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *key1, int *count1,
                      int *slot1, int *key2, int *count2, int *slot2, int *key3, int *count3,
                      int *slot3, uint32_t *pstart, void *pfrac, void *prel, bool fp32,
                      cudaStream_t s);
-// cpos[s] = prel[perm[s]] (float4 or double4): cell-relative positions in cell order.
+// cpos[s] = prel[perm[s]] (float4 or double4_32a): cell-relative positions in cell order.
 void launch_cell_gather(const void *prel, const int *perm, int n, bool fp32, void *cpos,
                         cudaStream_t s);
 // Real-space cell key (nc^3 cells of edge L/nc) and slot within its cell.
@@ -43,7 +43,7 @@ void launch_scatter(const int *key, const int *slot, const int *off, int n, int 
 template <typename T>
 void launch_records(const uint32_t *pstart, const T *pfrac, const int *perm, int n, int p,
                     int *rec_idx, uint32_t *rec_start, T *rec_w, cudaStream_t s);
-// Cell-sorted positions relative to their cell's lower corner (float4 or double4).
+// Cell-sorted positions relative to their cell's lower corner (float4 or double4_32a).
 void launch_cell_positions(const double *pos, const int *perm, int n, double L, int nc,
                            bool fp32, void *cpos, cudaStream_t s);
 
@@ -181,7 +181,7 @@ cudaError_t launch_zfft_influence(const CUtensorMap &map, T *G, const T *tab2, c
                                   cudaStream_t s);
 
 // ---- real-space pair sum + self term (realspace.cu) -----------------------
-// cpos: float4 for T = float, double4 for T = double (cell-relative).
+// cpos: float4 for T = float, double4_32a for T = double (cell-relative).
 template <typename T>
 cudaError_t launch_realspace(int nc, const int *cell_off, const int *cell_perm, const void *cpos,
                              const T *F, int R, double L, double rc, double xi, double a,

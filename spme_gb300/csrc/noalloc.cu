@@ -31,7 +31,6 @@
 // Errors: a pending error from the caller's earlier, unrelated launches is
 // cleared on entry (cudaGetLastError), so the status returned describes this
 // call's own work only.
-#include <mutex>
 
 #include "kernels.h"
 #include "spme_gb300.h"
@@ -50,7 +49,7 @@ constexpr size_t kOffKey = 0;
 constexpr size_t kOffSlot = kOffKey + align256(sizeof(int) * kMaxNp);
 constexpr size_t kOffPerm = kOffSlot + align256(sizeof(int) * kMaxNp);
 constexpr size_t kOffCpos = kOffPerm + align256(sizeof(int) * kMaxNp);
-constexpr size_t kOffF = kOffCpos + align256(sizeof(double4) * kMaxNp);
+constexpr size_t kOffF = kOffCpos + align256(sizeof(double4_32a) * kMaxNp);
 constexpr size_t kOffW = kOffF + align256(sizeof(double) * kMaxC * kMaxNp);
 constexpr size_t kOffCount = kOffW + align256(sizeof(double) * kMaxC * kMaxNp);
 constexpr size_t kOffOff = kOffCount + align256(sizeof(int) * kMaxCells);
@@ -59,29 +58,18 @@ constexpr size_t kScratchBytes = kOffTmp + align256(sizeof(int) * (kMaxCells / 2
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-unsigned char *g_scratch_addr[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
-
-// Device address of the scratch array on the current device (looked up once
-// per device; in host code the array's name is only a host-side stand-in).
+// Device address of the scratch array on the current device (in host code the
+// array's name is only a host-side stand-in).  Looked up on every call: cheap
+// once the module is loaded, legal during stream capture, and never stale
+// after a device reset reloads the module at another address.
 int scratch_address(unsigned char **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
         cudaGetLastError();
         return SPME_ERR_CUDA;
     }
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return SPME_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<unsigned char *>(p);
     return SPME_OK;
 }
 
@@ -115,7 +103,7 @@ extern "C" int spme_realspace_apply_noalloc(int np, const double *pos, double bo
     int *key = reinterpret_cast<int *>(base + kOffKey);
     int *slot = reinterpret_cast<int *>(base + kOffSlot);
     int *perm = reinterpret_cast<int *>(base + kOffPerm);
-    double4 *cpos = reinterpret_cast<double4 *>(base + kOffCpos);
+    double4_32a *cpos = reinterpret_cast<double4_32a *>(base + kOffCpos);
     double *F = reinterpret_cast<double *>(base + kOffF);
     double *W = reinterpret_cast<double *>(base + kOffW);
     int *count = reinterpret_cast<int *>(base + kOffCount);

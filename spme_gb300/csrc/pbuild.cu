@@ -38,7 +38,7 @@ __global__ void k_cell_keys(const double *__restrict__ pos, int n, double L, int
 // order later), so the FP64 coordinate arithmetic runs once per particle.
 template <typename T> struct Vec4T;
 template <> struct Vec4T<float> { using type = float4; };
-template <> struct Vec4T<double> { using type = double4; };
+template <> struct Vec4T<double> { using type = double4_32a; };
 
 template <typename T>
 __global__ void k_all_keys(const double *__restrict__ pos, int n, MeshGeom g, int nc,
@@ -277,7 +277,7 @@ void launch_all_keys(const double *pos, int n, const MeshGeom &g, int nc, int *k
     else
         k_all_keys<double><<<nblk(n, 256), 256, 0, s>>>(pos, n, g, nc, key1, count1, slot1, key2,
                                                         count2, slot2, key3, count3, slot3, pstart,
-                                                        (double *)pfrac, (double4 *)prel);
+                                                        (double *)pfrac, (double4_32a *)prel);
 }
 
 void launch_cell_gather(const void *prel, const int *perm, int n, bool fp32, void *cpos,
@@ -287,8 +287,8 @@ void launch_cell_gather(const void *prel, const int *perm, int n, bool fp32, voi
         k_cell_gather<float4><<<nblk(n, 256), 256, 0, s>>>((const float4 *)prel, perm, n,
                                                            (float4 *)cpos);
     else
-        k_cell_gather<double4><<<nblk(n, 256), 256, 0, s>>>((const double4 *)prel, perm, n,
-                                                            (double4 *)cpos);
+        k_cell_gather<double4_32a><<<nblk(n, 256), 256, 0, s>>>((const double4_32a *)prel, perm, n,
+                                                            (double4_32a *)cpos);
 }
 
 void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int *count,
@@ -331,8 +331,8 @@ void launch_cell_positions(const double *pos, const int *perm, int n, double L, 
         k_cell_positions<float4, float><<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, nc,
                                                                     (float4 *)cpos);
     else
-        k_cell_positions<double4, double><<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, nc,
-                                                                      (double4 *)cpos);
+        k_cell_positions<double4_32a, double><<<nblk(n, 256), 256, 0, s>>>(pos, perm, n, L, nc,
+                                                                      (double4_32a *)cpos);
 }
 
 template void launch_records<float>(const uint32_t *, const float *, const int *, int, int, int *,

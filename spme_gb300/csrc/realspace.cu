@@ -205,7 +205,7 @@ __device__ __forceinline__ PairSum<T> shfl_xor(const PairSum<T> &a, int o) {
 
 template <typename G> struct Geo4;
 template <> struct Geo4<float> { using type = float4; };
-template <> struct Geo4<double> { using type = double4; };
+template <> struct Geo4<double> { using type = double4_32a; };
 
 __device__ __forceinline__ float d_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double d_rint(double x) { return rint(x); }
@@ -265,8 +265,8 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     __shared__ float fx[kPre ? kCap : 1], fy[kPre ? kCap : 1], fz[kPre ? kCap : 1];
     __shared__ int hits[kWarps][64];
     // one record per buffered pair: unit vector and F in one 16/32-byte vector,
-    // then G and the start of the partner's force row
-    struct __align__(16) PairRec {
+    // then G and the start of the partner's force row (aligned as that vector)
+    struct PairRec {
         typename Geo4<T>::type rf;  // (rhat_x, rhat_y, rhat_z, F)
         const T *frow;
         T gfac;

@@ -70,7 +70,7 @@ __device__ __forceinline__ void zpass(Cx<T> *__restrict__ sb, int Kr, int Lr,
     const bool unit1 = L == 1;
     DivMod dl;
     if constexpr (LC == 0) dl.init(L);
-#pragma unroll(KC ? 4 : 1)
+#pragma unroll(KC ? 2 : 1)
     for (int bi = bi0; bi < nb; bi += BS) {
         int j, b;
         if constexpr (LC != 0) {
@@ -239,7 +239,6 @@ constexpr ZCfg kCfg64[] = {{8, 384, 1, 6}, {4, 192, 2, 12}, {8, 192, 1, 12},
 template <int KS>
 struct ZFixed {
     static constexpr int n = 0;
-    static constexpr int code[1] = {0}, span[1] = {0};
 };
 template <>
 struct ZFixed<128> {
