@@ -77,6 +77,25 @@ def test_recip_fp64_vs_oracle(gpu_lib, case):
     assert relerr(u, ref) < FP64_TOL
 
 
+@pytest.mark.parametrize("precision,K,tol", [("fp64", 300, FP64_TOL), ("fp32", 320, 1e-5)])
+def test_recip_large_mesh_vs_oracle(gpu_lib, precision, K, tol):
+    """K = 300 and 320: the fused z-transform kernel runs its narrow-chunk
+    configuration here (2 columns per block in FP64, 4 in FP32, the sizes it
+    serves from K = 296 to about 1100), with the runtime radix-3/5 pass sequence
+    at K = 300."""
+    n, L, p, xi, R = 3000, 60.0, 6, 0.5, 2
+    pos, f = uniform_case(n, L, R, seed=K + n)
+    eng = spme_gb300.Engine(n, L, xi, K, p, precision=precision, max_nrhs=R,
+                            terms=spme_gb300.TERM_RECIP)
+    eng.set_positions(pos)
+    u = eng.apply(f.astype(eng.dtype)).astype(np.float64)
+    eng.close()
+    ref = oracle.recip(pos, L, xi, K, p, f.astype(eng.dtype).astype(np.float64))
+    err = relerr(u, ref)
+    print(f"K={K} {precision}: rel-L2 vs oracle {err:.2e}")
+    assert err < tol
+
+
 @pytest.mark.parametrize("tile", [(4, 4, 4), (8, 8, 8), (16, 8, 4), (16, 16, 4), (8, 16, 8)])
 def test_tile_shapes(gpu_lib, tile):
     n, L, K, p, xi = 700, 30.0, 40, 6, 0.4
