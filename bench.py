@@ -242,6 +242,39 @@ def cpu_baseline_time(w, nth=None, single_thread=True):
     return out
 
 
+def cpu_baseline_batch(systems, nth=None):
+    """CPU baseline of the uneven batch on the host cores: the reference's own
+    compute_spme (compiled unmodified, coloured OpenMP spread, all cores) on each
+    system inside its domain (p in {4, 6}, even K, 4p < K), plus the oracle's
+    real-space/self sum it lacks; one right-hand side per system, one rep.
+    None when the reference build is absent."""
+    if not _ref_lib_available():
+        return None
+    nth = nth or (os.cpu_count() or 1)
+    total, parts, used = 0.0, 0, 0
+    for k, s in enumerate(systems):
+        if not (s["p"] in (4, 6) and s["K"] % 2 == 0 and 4 * s["p"] < s["K"]):
+            continue
+        rng = np.random.default_rng(500 + k)
+        pos = rng.uniform(0.0, s["L"], size=(s["N"], 3))
+        f1 = rng.standard_normal((1, 3 * s["N"]))
+        wk = {"N": s["N"], "L": s["L"], "K": s["K"], "p": s["p"], "xi": s["xi"],
+              "rc": s["rc"], "a": s["radius"]}
+        t_rec, _ = _reference_recip_time(wk, pos, f1, nth, 1)
+        total += t_rec + _real_self_time(wk, pos, f1, nth, 1)
+        parts += s["N"]
+        used += 1
+    if used == 0:
+        return None
+    return {"value": total * 1e9 / parts, "unit": UNIT, "cores": nth, "kind": "reference",
+            "sample": f"{used} of {len(systems)} systems (those in the reference's domain: p in "
+                      "{4, 6}, even K, 4p < K; the GPU value covers all systems), 1 right-hand "
+                      "side each, one rep: the reference's compute_spme compiled unmodified "
+                      "(coloured OpenMP spread, project DFTI shim for MKL) + the oracle's "
+                      "real-space/self sum (absent from the reference)",
+            "systems": used, "particles": parts}
+
+
 def run_reference(args, w):
     """The reference's CPU path on the host cores for the same workload: per step
     one right-hand side of the full system with new positions (the reference's
@@ -563,7 +596,9 @@ def run_secondary(args):
     out = {}
     for wl in ("scale_up", "multi_rhs", "uneven_batch"):
         cmd = [sys.executable, os.path.abspath(__file__), "--workload", wl, "--steps",
-               str(max(5, args.steps)), "--warmup", "3", "--no-cpu-baseline", "--no-secondary"]
+               str(max(5, args.steps)), "--warmup", "3", "--no-secondary"]
+        if args.no_cpu_baseline:
+            cmd.append("--no-cpu-baseline")
         try:
             r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
             d = json.loads([x for x in r.stdout.splitlines() if x.startswith("{")][-1])
@@ -573,7 +608,7 @@ def run_secondary(args):
         keep = ("value", "unit", "ms_per_step", "config", "e2e", "kernels", "per_system_loop",
                 "engines_graph", "speedup_vs_loop", "speedup_vs_engines_graph",
                 "stages_ms_serialized", "gpu_launches", "autotune", "fp64_plain",
-                "fp32_batched_speedup_vs_fp64_plain", "accuracy", "clocks")
+                "fp32_batched_speedup_vs_fp64_plain", "accuracy", "cpu_baseline", "clocks")
         out[wl] = {k: d[k] for k in keep if k in d}
     return out
 
@@ -592,6 +627,8 @@ def run_batch(args, w):
     systems = uneven_systems(count=w["count"], xi=w["xi"], rc=w["rc"], radius=w["a"],
                              seed=1234 + rank)
     R = w["R"]
+    cpu_base = (cpu_baseline_batch(systems)
+                if rank == 0 and ws == 1 and not args.no_cpu_baseline else None)
     rng = np.random.default_rng(77 + rank)
     pos = [torch.tensor(rng.uniform(0, s["L"], (s["N"], 3)), device="cuda") for s in systems]
     f = [torch.tensor(rng.standard_normal((R, 3 * s["N"])), dtype=torch.float32, device="cuda")
@@ -650,6 +687,7 @@ def run_batch(args, w):
         "speedup_vs_loop": loop_ms / ms,
         "speedup_vs_engines_graph": graph_ms / ms,
         "autotune": ({"tile": list(b.tuned[0]), "overlap": b.tuned[1]} if b.tuned else None),
+        "cpu_baseline": cpu_base,
         "clocks": ck,
     }
     print(json.dumps(line), flush=True)
