@@ -487,7 +487,9 @@ int build_tiles(_spme_batch_t *b) {
         A.cb = 0;
         A.ce = b->C;
         A.accumulate = 0;
-        A.use_tma = 0;
+        // TMA boxes where the mesh rows allow them (K a multiple of 16 bytes / elem);
+        // plain-load staging otherwise
+        A.use_tma = make_interp_box(&is[k].tmap, A.mesh, b->C, x.g, sizeof(T)) ? 1 : 0;
         A.ws = b->ws;
         pre[k + 1] = pre[k] + x.g.ntx * x.g.nty * x.g.ntz;
     }

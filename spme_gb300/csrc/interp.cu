@@ -212,12 +212,15 @@ k_interp_batch(const InterpSys<T> *__restrict__ sys, const int *__restrict__ pre
                int total) {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int k = batch_find(prefix, nsys, w);
-        const InterpSys<T> S = sys[k];
+        const InterpArgs<T> A = sys[k].args;
+        // the system's TMA box stays in the global work list (a descriptor in
+        // global memory; never a local copy)
+        const CUtensorMap *tmap = A.use_tma ? &sys[k].tmap : nullptr;
         const int tile = w - prefix[k];
-        switch (S.args.g.p) {
-            case 4: interp_body<T, 4, CG>(nullptr, S.args, tile); break;
-            case 6: interp_body<T, 6, CG>(nullptr, S.args, tile); break;
-            default: interp_body<T, 8, CG>(nullptr, S.args, tile); break;
+        switch (A.g.p) {
+            case 4: interp_body<T, 4, CG>(tmap, A, tile); break;
+            case 6: interp_body<T, 6, CG>(tmap, A, tile); break;
+            default: interp_body<T, 8, CG>(tmap, A, tile); break;
         }
         __syncthreads();
     }
@@ -277,6 +280,10 @@ bool encode_box(CUtensorMap *m, const void *mesh, int K, int C, const MeshGeom &
 
 size_t interp_smem_bytes(const MeshGeom &g, size_t elem) {
     return (size_t)4 * (g.tz + g.p - 1) * (g.ty + g.p - 1) * kHX * elem + 128;
+}
+
+bool make_interp_box(CUtensorMap *map, const void *mesh, int C, const MeshGeom &g, size_t elem) {
+    return encode_box(map, mesh, g.K, C, g, elem, 4);
 }
 
 bool make_interp_maps(InterpMaps *maps, const void *mesh, int C, const MeshGeom &g, size_t elem) {

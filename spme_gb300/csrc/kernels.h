@@ -113,10 +113,17 @@ struct InterpArgs {
     MeshGeom g;
     int C, cb, ce, accumulate, use_tma, ws;
 };
+// One system of a batched interpolation: its arguments and, when args.use_tma
+// is set, its 4-component TMA box over its own mesh (make_interp_box; read by
+// the kernel from this global work list, 64-byte aligned).
 template <typename T>
 struct InterpSys {
+    CUtensorMap tmap;
     InterpArgs<T> args;
 };
+// The 4-component TMA box of one mesh (false where TMA does not apply: K * elem
+// not a multiple of 16 bytes, an unaligned mesh, or no driver entry point).
+bool make_interp_box(CUtensorMap *map, const void *mesh, int C, const MeshGeom &g, size_t elem);
 // All systems in one persistent launch over their tiles (prefix as for the
 // spread; smem = the largest interp_smem_bytes of the systems).
 template <typename T>
