@@ -372,8 +372,15 @@ struct _spme_batch_t {
     InflSys *d_infl_sys = nullptr;
     int *d_pre_spread = nullptr, *d_pre_interp = nullptr, *d_pre_real = nullptr,
         *d_pre_infl = nullptr;
-    int tot_spread = 0, tot_interp = 0, tot_real = 0, tot_infl = 0;
-    size_t interp_smem = 0;
+    int tot_spread = 0, tot_real = 0, tot_infl = 0;
+    // interpolation work lists, one per B-spline order: each group is one launch
+    // with its own shared-memory size (a p = 8 box would otherwise set the
+    // occupancy of every system)
+    struct InterpGroup {
+        int first = 0, count = 0, pre_off = 0, total = 0;
+        size_t smem = 0;
+    };
+    std::vector<InterpGroup> igroups;
     // one captured graph of set_positions + apply
     bool use_graphs = false;
     cudaGraphExec_t gexec = nullptr;
@@ -469,12 +476,30 @@ int build_tiles(_spme_batch_t *b) {
     b->ntile_keys = off;
     BTRY(balloc(&b->d_cnt1, sizeof(int) * off));
     BTRY(balloc(&b->d_off1, sizeof(int) * (off + 1)));
-    b->interp_smem = smem;
+    // systems ordered by p, one work list (and prefix) per order
+    std::vector<int> order(b->nsys);
+    for (int k = 0; k < b->nsys; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int i, int j) {
+        return b->sys[i].s.porder < b->sys[j].s.porder;
+    });
+    b->igroups.clear();
     std::vector<InterpSys<T>> is(b->nsys);
-    std::vector<int> pre(b->nsys + 1, 0);
-    for (int k = 0; k < b->nsys; k++) {
+    std::vector<int> pre;
+    pre.reserve(b->nsys + 3);
+    for (int q = 0; q < b->nsys; q++) {
+        const int k = order[q];
         const BatchSys &x = b->sys[k];
-        InterpArgs<T> &A = is[k].args;
+        if (b->igroups.empty() || b->sys[order[q - 1]].s.porder != x.s.porder) {
+            typename _spme_batch_t::InterpGroup grp;
+            grp.first = q;
+            grp.pre_off = (int)pre.size();
+            b->igroups.push_back(grp);
+            pre.push_back(0);
+        }
+        auto &grp = b->igroups.back();
+        grp.count++;
+        grp.smem = std::max(grp.smem, interp_smem_bytes(x.g, sizeof(T)));
+        InterpArgs<T> &A = is[q].args;
         A.tile_off = b->d_off1 + x.tile_off;
         A.rec_idx = b->d_ridx1;
         A.rec_start = b->d_rst1;
@@ -489,14 +514,16 @@ int build_tiles(_spme_batch_t *b) {
         A.accumulate = 0;
         // TMA boxes where the mesh rows allow them (K a multiple of 16 bytes / elem);
         // plain-load staging otherwise
-        A.use_tma = make_interp_box(&is[k].tmap, A.mesh, b->C, x.g, sizeof(T)) ? 1 : 0;
+        A.use_tma = make_interp_box(&is[q].tmap, A.mesh, b->C, x.g, sizeof(T)) ? 1 : 0;
         A.ws = b->ws;
-        pre[k + 1] = pre[k] + x.g.ntx * x.g.nty * x.g.ntz;
+        grp.total += x.g.ntx * x.g.nty * x.g.ntz;
+        pre.push_back(grp.total);
     }
-    b->tot_interp = pre[b->nsys];
+    // orders are 4, 6 or 8 (validate_sys): at most three groups, nsys + 3 prefix entries
+    if (pre.size() > (size_t)b->nsys + 3) return SPME_ERR_INVALID;
     BTRY_CUDA(cudaMemcpy(b->d_interp_sys, is.data(), sizeof(InterpSys<T>) * b->nsys,
                          cudaMemcpyHostToDevice));
-    BTRY_CUDA(cudaMemcpy(b->d_pre_interp, pre.data(), sizeof(int) * (b->nsys + 1),
+    BTRY_CUDA(cudaMemcpy(b->d_pre_interp, pre.data(), sizeof(int) * pre.size(),
                          cudaMemcpyHostToDevice));
     std::vector<BatchGeo> geo(b->nsys);
     for (int k = 0; k < b->nsys; k++) {
@@ -586,7 +613,7 @@ int create_t(_spme_batch_t *b) {
     BTRY(balloc(&b->d_real_sys, sizeof(RealArgs<T>) * ns));
     BTRY(balloc(&b->d_infl_sys, sizeof(InflSys) * ns));
     BTRY(balloc(&b->d_pre_spread, sizeof(int) * (ns + 1)));
-    BTRY(balloc(&b->d_pre_interp, sizeof(int) * (ns + 1)));
+    BTRY(balloc(&b->d_pre_interp, sizeof(int) * (ns + 3)));  // a prefix per order group
     BTRY(balloc(&b->d_pre_real, sizeof(int) * (ns + 1)));
     BTRY(balloc(&b->d_pre_infl, sizeof(int) * (ns + 1)));
 
@@ -816,8 +843,14 @@ int apply_body(_spme_batch_t *b, double alpha, const T *f, double beta, T *u) {
     mark(b, 6);
     BTRY(run_ffts<T>(b, true, fconc));
     mark(b, 7);
-    BTRY_CUDA(launch_interp_batch<T>((const InterpSys<T> *)b->d_interp_sys, b->d_pre_interp,
-                                     b->nsys, b->tot_interp, b->interp_smem, s));
+    // the kernel's shared-memory limit covers every group (a captured graph replays
+    // all the launches against the limit last set)
+    size_t smem_max = 0;
+    for (const auto &grp : b->igroups) smem_max = std::max(smem_max, grp.smem);
+    for (const auto &grp : b->igroups)
+        BTRY_CUDA(launch_interp_batch<T>((const InterpSys<T> *)b->d_interp_sys + grp.first,
+                                         b->d_pre_interp + grp.pre_off, grp.count, grp.total,
+                                         grp.smem, s, smem_max));
     mark(b, 8);
     if (conc) BTRY_CUDA(cudaStreamWaitEvent(s, b->ev_rs_join, 0));
     k_batch_unpack<T><<<grid_cap(total, 256, 8), 256, 0, s>>>(
@@ -825,7 +858,7 @@ int apply_body(_spme_batch_t *b, double alpha, const T *f, double beta, T *u) {
         (T)beta, u);
     mark(b, 9);
     b->stages_valid = b->profiling;
-    b->launches += 7;
+    b->launches += 6 + (long)b->igroups.size();
     return from_cuda(cudaGetLastError());
 }
 

@@ -309,11 +309,11 @@ cudaError_t launch_interp(const InterpMaps &maps, const int *tile_off, int n, co
 
 template <typename T>
 cudaError_t launch_interp_batch(const InterpSys<T> *sys, const int *prefix, int nsys, int total,
-                                size_t smem, cudaStream_t s) {
+                                size_t smem, cudaStream_t s, size_t smem_limit) {
     if (total <= 0) return cudaSuccess;
     auto kern = k_interp_batch<T, 4>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+                                         (int)std::max(smem, smem_limit));
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -325,9 +325,9 @@ cudaError_t launch_interp_batch(const InterpSys<T> *sys, const int *prefix, int 
 }
 
 template cudaError_t launch_interp_batch<float>(const InterpSys<float> *, const int *, int, int,
-                                                size_t, cudaStream_t);
+                                                size_t, cudaStream_t, size_t);
 template cudaError_t launch_interp_batch<double>(const InterpSys<double> *, const int *, int, int,
-                                                 size_t, cudaStream_t);
+                                                 size_t, cudaStream_t, size_t);
 template cudaError_t launch_interp<float>(const InterpMaps &, const int *, int, const int *,
                                           const uint32_t *, const float *, const float *, int,
                                           int, int, const MeshGeom &, float *, int, int *,

@@ -125,10 +125,11 @@ struct InterpSys {
 // not a multiple of 16 bytes, an unaligned mesh, or no driver entry point).
 bool make_interp_box(CUtensorMap *map, const void *mesh, int C, const MeshGeom &g, size_t elem);
 // All systems in one persistent launch over their tiles (prefix as for the
-// spread; smem = the largest interp_smem_bytes of the systems).
+// spread; smem = the largest interp_smem_bytes of the systems; the kernel's
+// dynamic shared-memory limit is set to max(smem, smem_limit)).
 template <typename T>
 cudaError_t launch_interp_batch(const InterpSys<T> *sys, const int *prefix, int nsys, int total,
-                                size_t smem, cudaStream_t s);
+                                size_t smem, cudaStream_t s, size_t smem_limit = 0);
 // Components [cb, ce) of the C-component mesh (cb a multiple of 4) into
 // W[n][C]; err: device flag set to 1 if a TMA wait timed out.
 template <typename T>
