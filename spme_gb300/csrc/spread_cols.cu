@@ -489,22 +489,50 @@ k_spread_cols_batch(const SpreadColsSys<T> *__restrict__ sys, const int *__restr
 // (0 where that component does not exist or k >= CPL); CPL = 1: Fs[s][c] = F[idx[s]][c].
 template <typename T, int CPL>
 __global__ void k_gather_cols_rows(const T *__restrict__ F, const int *__restrict__ idx, int n,
-                                   int C, int RW, T *__restrict__ Fs) {
+                                   int C, int RW, int nchunk, T *__restrict__ Fs) {
+    // one thread per (slot, chunk, lane): the lane's CPL components (padded to PC)
+    // as one vector store
     constexpr int PC = cols_pcpl(CPL);
-    const size_t total = (size_t)n * RW;
+    const size_t total = (size_t)n * nchunk * 16;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = t / RW;
-        const int q = (int)(t - s * RW);
-        int c;
-        if (CPL == 1) {
-            c = q;
+        const int l = (int)(t & 15);
+        const size_t sc = t >> 4;  // (slot, chunk)
+        const size_t s = nchunk == 1 ? sc : sc / nchunk;
+        const int chunk = (int)(sc - s * nchunk);
+        const T *src = F + (size_t)__ldg(idx + s) * C;
+        if constexpr (CPL == 1) {
+            if (l < C) Fs[s * RW + l] = __ldg(src + l);
         } else {
-            const int chunk = q / (16 * PC), r = q - chunk * 16 * PC;
-            const int l = r / PC, k = r - l * PC;
-            c = k < CPL ? chunk * 16 * CPL + l + 16 * k : C;
+            T v[PC];
+#pragma unroll
+            for (int k = 0; k < PC; k++) {
+                const int c = chunk * 16 * CPL + l + 16 * k;
+                v[k] = (k < CPL && c < C) ? __ldg(src + c) : T(0);
+            }
+            T *dst = Fs + s * RW + (size_t)chunk * 16 * PC + (size_t)l * PC;
+            using V = typename V16<T>::type;  // 16 bytes: float4 or double2
+            constexpr int VW = 16 / (int)sizeof(T);
+            if constexpr (PC * sizeof(T) >= 16) {
+#pragma unroll
+                for (int q = 0; q < PC / VW; q++) {
+                    V w;
+                    if constexpr (VW == 4) {
+                        w.x = v[4 * q];
+                        w.y = v[4 * q + 1];
+                        w.z = v[4 * q + 2];
+                        w.w = v[4 * q + 3];
+                    } else {
+                        w.x = v[2 * q];
+                        w.y = v[2 * q + 1];
+                    }
+                    reinterpret_cast<V *>(dst)[q] = w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < PC; k++) dst[k] = v[k];
+            }
         }
-        Fs[t] = c < C ? F[(size_t)idx[s] * C + c] : T(0);
     }
 }
 
@@ -588,17 +616,22 @@ int spread_cols_row_width(int C) {
 template <typename T>
 void launch_gather_cols_rows(const T *F, const int *idx, int n, int C, T *Fs, cudaStream_t s) {
     const int RW = spread_cols_row_width(C);
-    const size_t total = (size_t)n * RW;
-    if (!total) return;
-    switch (cols_cpl(C)) {
+    const int cpl = cols_cpl(C);
+    const int nchunk = cpl == 1 ? 1 : RW / (16 * cols_pcpl(cpl));
+    const size_t total = (size_t)n * nchunk * 16;  // threads: (slot, chunk, lane)
+    if (n <= 0) return;
+    switch (cpl) {
         case 1:
-            k_gather_cols_rows<T, 1><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW, Fs);
+            k_gather_cols_rows<T, 1><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW,
+                                                                            nchunk, Fs);
             break;
         case 2:
-            k_gather_cols_rows<T, 2><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW, Fs);
+            k_gather_cols_rows<T, 2><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW,
+                                                                            nchunk, Fs);
             break;
         default:
-            k_gather_cols_rows<T, 3><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW, Fs);
+            k_gather_cols_rows<T, 3><<<blocks_for_rows(total), 256, 0, s>>>(F, idx, n, C, RW,
+                                                                            nchunk, Fs);
             break;
     }
 }
