@@ -139,41 +139,82 @@ k_batch_records(const uint32_t *__restrict__ pstart, const T *__restrict__ pfrac
 }
 
 // Caller layout (system k at element 3 R P_k, rows of 3 N_k) <-> packed rows
-// F[i][3R]; one thread per element of the caller's layout, the system found
-// from the particle prefix (element t of the caller's layout belongs to
-// particle range t / 3R).
+// F[i][3R]; one thread per particle (its system found once from the particle
+// prefix), four right-hand sides at a time as three 16-byte vectors on the
+// packed side where R is a multiple of 4 (FP32), scalars otherwise.
 template <typename T>
 __global__ void k_batch_pack(const T *__restrict__ f, const int *__restrict__ pref, int nsys,
-                             int R, long total, T *__restrict__ F) {
+                             int R, int ntot, T *__restrict__ F) {
     const int C = 3 * R;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long)gridDim.x * blockDim.x) {
-        const int k = batch_find(pref, nsys, (int)(t / C));
-        const int P0 = pref[k], nk = pref[k + 1] - P0;
-        const long q = t - (long)C * P0;
-        const int r = (int)(q / (3L * nk));
-        const int rem = (int)(q - (long)r * 3 * nk);
-        const int li = rem / 3, d = rem - 3 * li;
-        F[(size_t)(P0 + li) * C + 3 * r + d] = f[t];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += gridDim.x * blockDim.x) {
+        const int k = batch_find(pref, nsys, i);
+        const int P0 = pref[k], nk = pref[k + 1] - P0, li = i - P0;
+        const T *src = f + (size_t)C * P0 + 3 * li;
+        T *dst = F + (size_t)i * C;
+        int r = 0;
+        if constexpr (sizeof(T) == 4) {
+            if ((R & 3) == 0) {
+                for (; r < R; r += 4) {
+                    float v[12];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const T *s = src + (size_t)(r + q) * 3 * nk;
+                        v[3 * q] = __ldg(s);
+                        v[3 * q + 1] = __ldg(s + 1);
+                        v[3 * q + 2] = __ldg(s + 2);
+                    }
+                    float4 *d4 = reinterpret_cast<float4 *>(dst + 3 * r);
+                    d4[0] = make_float4(v[0], v[1], v[2], v[3]);
+                    d4[1] = make_float4(v[4], v[5], v[6], v[7]);
+                    d4[2] = make_float4(v[8], v[9], v[10], v[11]);
+                }
+            }
+        }
+        for (; r < R; r++) {
+            const T *s = src + (size_t)r * 3 * nk;
+            dst[3 * r] = __ldg(s);
+            dst[3 * r + 1] = __ldg(s + 1);
+            dst[3 * r + 2] = __ldg(s + 2);
+        }
     }
 }
 
 template <typename T>
 __global__ void k_batch_unpack(const T *__restrict__ W, const T *__restrict__ W2,
-                               const int *__restrict__ pref, int nsys, int R, long total, T alpha,
+                               const int *__restrict__ pref, int nsys, int R, int ntot, T alpha,
                                T beta, T *__restrict__ u) {
     const int C = 3 * R;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long)gridDim.x * blockDim.x) {
-        const int k = batch_find(pref, nsys, (int)(t / C));
-        const int P0 = pref[k], nk = pref[k + 1] - P0;
-        const long q = t - (long)C * P0;
-        const int r = (int)(q / (3L * nk));
-        const int rem = (int)(q - (long)r * 3 * nk);
-        const int li = rem / 3, d = rem - 3 * li;
-        const size_t j = (size_t)(P0 + li) * C + 3 * r + d;
-        const T w = W[j] + W2[j];
-        u[t] = beta == T(0) ? alpha * w : beta * u[t] + alpha * w;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += gridDim.x * blockDim.x) {
+        const int k = batch_find(pref, nsys, i);
+        const int P0 = pref[k], nk = pref[k + 1] - P0, li = i - P0;
+        T *dst = u + (size_t)C * P0 + 3 * li;
+        const size_t row = (size_t)i * C;
+        auto put = [&](int r, int d, T w) {
+            T *o = dst + (size_t)r * 3 * nk + d;
+            *o = beta == T(0) ? alpha * w : beta * *o + alpha * w;
+        };
+        int r = 0;
+        if constexpr (sizeof(T) == 4) {
+            if ((R & 3) == 0) {
+                for (; r < R; r += 4) {
+                    const float4 *a4 = reinterpret_cast<const float4 *>(W + row + 3 * r);
+                    const float4 *b4 = reinterpret_cast<const float4 *>(W2 + row + 3 * r);
+                    float v[12];
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        const float4 a = __ldg(a4 + q), bb = __ldg(b4 + q);
+                        v[4 * q] = a.x + bb.x;
+                        v[4 * q + 1] = a.y + bb.y;
+                        v[4 * q + 2] = a.z + bb.z;
+                        v[4 * q + 3] = a.w + bb.w;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 12; q++) put(r + q / 3, q % 3, v[q]);
+                }
+            }
+        }
+        for (; r < R; r++)
+            for (int d = 0; d < 3; d++) put(r, d, W[row + 3 * r + d] + W2[row + 3 * r + d]);
     }
 }
 
@@ -222,12 +263,14 @@ k_batch_influence(Cx2<T> *__restrict__ G_all, const T *__restrict__ tab_all,
         const T tl = (T)S.twopi_L;
         const int local = w - prefix[k];
         if (local < S.nb_int) {
-            const size_t kidx = (size_t)local * 256 + threadIdx.x;
-            if (kidx >= Kc) continue;
-            const int x = (int)(kidx % Kh);
+            // a system's half spectrum has fewer than 2^31 points (K <= 1024):
+            // 32-bit index arithmetic
+            const unsigned kidx = (unsigned)local * 256u + threadIdx.x;
+            if (kidx >= (unsigned)Kc) continue;
+            const unsigned rest = kidx / (unsigned)Kh;
+            const int x = (int)(kidx - rest * (unsigned)Kh);
             if (x == 0 || (!(K & 1) && x == K / 2)) continue;
-            const size_t rest = kidx / Kh;
-            const int y = (int)(rest % K), z = (int)(rest / K);
+            const int z = (int)(rest / (unsigned)K), y = (int)(rest - (unsigned)z * (unsigned)K);
             const V2 mc = tab[kidx];
             const T kx = (T)x * tl;
             const T ky = (T)(y <= K / 2 ? y : y - K) * tl;
@@ -815,8 +858,8 @@ int apply_body(_spme_batch_t *b, double alpha, const T *f, double beta, T *u) {
     const int n = b->ntot, C = b->C;
     const long total = (long)n * C;
     mark(b, 1);  // (the position build, when it ran, ends here)
-    k_batch_pack<T><<<grid_cap(total, 256, 8), 256, 0, s>>>(f, b->d_pref, b->nsys, b->R, total,
-                                                           (T *)b->d_F);
+    k_batch_pack<T><<<grid_cap(n, 256, 8), 256, 0, s>>>(f, b->d_pref, b->nsys, b->R, n,
+                                                       (T *)b->d_F);
     mark(b, 2);
     // the real-space sum beside the mesh pipeline when asked (serially when
     // profiling, so that every stage is timed alone)
@@ -853,8 +896,8 @@ int apply_body(_spme_batch_t *b, double alpha, const T *f, double beta, T *u) {
                                          grp.smem, s, smem_max));
     mark(b, 8);
     if (conc) BTRY_CUDA(cudaStreamWaitEvent(s, b->ev_rs_join, 0));
-    k_batch_unpack<T><<<grid_cap(total, 256, 8), 256, 0, s>>>(
-        (const T *)b->d_W, (const T *)b->d_W2, b->d_pref, b->nsys, b->R, total, (T)alpha,
+    k_batch_unpack<T><<<grid_cap(n, 256, 8), 256, 0, s>>>(
+        (const T *)b->d_W, (const T *)b->d_W2, b->d_pref, b->nsys, b->R, n, (T)alpha,
         (T)beta, u);
     mark(b, 9);
     b->stages_valid = b->profiling;
