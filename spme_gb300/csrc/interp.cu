@@ -204,8 +204,10 @@ k_interp(const __grid_constant__ CUtensorMap tmap, InterpArgs<T> A) {
     interp_body<T, P, CG>(&tmap, A, blockIdx.x);
 }
 
-// Many systems in one persistent launch over their tiles (plain-load staging,
-// no TMA); the order p of each system selects the body.
+// Many systems in one persistent launch over their tiles: each system's boxes
+// by TMA through its own descriptor in the work list where its mesh rows allow
+// it, by plain loads otherwise; the order p of each system selects the body
+// (the batch launches one such kernel per order).
 template <typename T, int CG>
 __global__ void __launch_bounds__(kThreads)
 k_interp_batch(const InterpSys<T> *__restrict__ sys, const int *__restrict__ prefix, int nsys,
