@@ -114,6 +114,19 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
         __syncthreads();
     };
 
+    // the warp's first particle's record, the same for every component chunk:
+    // loaded once, before the first box is waited for
+    constexpr int kWarps = kThreads / 32;
+    T wreg_0 = T(0);
+    uint32_t st_0 = 0;
+    int idx_0 = 0;
+    if (pbeg + warp < pend) {
+        const int s = pbeg + warp;
+        wreg_0 = lane < 3 * P ? __ldg(rec_w + (size_t)s * WS + lane) : T(0);
+        st_0 = __ldg(rec_start + s);
+        idx_0 = __ldg(rec_idx + s);
+    }
+
     int chunk = 0;
     for (int c0 = cb; c0 < ce; c0 += CG, chunk++) {
         const int nc = min(CG, ce - c0);
@@ -133,16 +146,9 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
             stage_rows(c0, nc, false);
         }
         // the next particle's record is loaded while this one is interpolated
-        constexpr int kWarps = kThreads / 32;
-        T wreg_n = T(0);
-        uint32_t st_n = 0;
-        int idx_n = 0;
-        if (pbeg + warp < pend) {
-            const int s = pbeg + warp;
-            wreg_n = lane < 3 * P ? __ldg(rec_w + (size_t)s * WS + lane) : T(0);
-            st_n = __ldg(rec_start + s);
-            idx_n = __ldg(rec_idx + s);
-        }
+        T wreg_n = wreg_0;
+        uint32_t st_n = st_0;
+        int idx_n = idx_0;
         for (int s = pbeg + warp; s < pend; s += kWarps) {
             const T wreg = wreg_n;
             const uint32_t st = st_n;
@@ -199,7 +205,8 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
 }
 
 template <typename T, int P, int CG>
-__global__ void __launch_bounds__(kThreads)
+// blocks per SM that the 4-component box's shared memory allows (16x8x4 tiles)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 5 : 2)
 k_interp(const __grid_constant__ CUtensorMap tmap, InterpArgs<T> A) {
     interp_body<T, P, CG>(&tmap, A, blockIdx.x);
 }
