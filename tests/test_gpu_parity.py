@@ -77,6 +77,23 @@ def test_recip_fp64_vs_oracle(gpu_lib, case):
     assert relerr(u, ref) < FP64_TOL
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
+def test_small_box_single_cell_real_space(gpu_lib, precision, tol):
+    """L < 3 rc: the real-space sum runs over one cell with minimum images (two
+    cells per side here, L = 25, rc = 10), full operator against the oracle."""
+    n, L, K, p, xi, rc, R = 300, 25.0, 24, 6, 0.35, 10.0, 2
+    pos, f = uniform_case(n, L, R, seed=25)
+    eng = spme_gb300.Engine(n, L, xi, K, p, rcut=rc, precision=precision, max_nrhs=R)
+    eng.set_positions(pos)
+    fin = f.astype(eng.dtype)
+    u = eng.apply(fin).astype(np.float64)
+    eng.close()
+    ref = oracle.full(pos, L, xi, rc, K, p, fin.astype(np.float64), nthreads=4)
+    err = relerr(u, ref)
+    print(f"single-cell {precision}: rel-L2 vs oracle {err:.2e}")
+    assert err < tol
+
+
 @pytest.mark.parametrize("precision,K,tol", [("fp64", 300, FP64_TOL), ("fp32", 320, 1e-5)])
 def test_recip_large_mesh_vs_oracle(gpu_lib, precision, K, tol):
     """K = 300 and 320: the fused z-transform kernel runs its narrow-chunk
