@@ -263,7 +263,10 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
     // test then runs only on candidates that pass it)
     constexpr bool kPre = sizeof(G) == 8;
     __shared__ float fx[kPre ? kCap : 1], fy[kPre ? kCap : 1], fz[kPre ? kCap : 1];
-    __shared__ int hits[kWarps][64];
+    // candidates tested per lane per iteration (FP32: 2; FP64 keeps 1, its shared
+    // memory is at the 8-blocks-per-SM limit)
+    constexpr int kU = sizeof(T) == 4 ? 2 : 1;
+    __shared__ int hits[kWarps][32 + 32 * kU];  // up to 31 carried + 32 kU new
     // one record per buffered pair: unit vector and F in one 16/32-byte vector,
     // then G and the start of the partner's force row (aligned as that vector)
     struct PairRec {
@@ -429,8 +432,8 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
                 }
                 __syncwarp();
             };
-            for (int q0 = 0; q0 < ncand; q0 += 32) {
-                const int q = q0 + lane;
+            // candidate q within rc of particle i (and not i itself)
+            auto test = [&](int q) {
                 bool hit = false;
                 bool maybe = q < ncand;
                 if (pre && maybe) {
@@ -452,18 +455,39 @@ __device__ __forceinline__ void realspace_body(const RealArgs<T> &A, int cell) {
                         hit = d0 * d0 + d1 * d1 + d2 * d2 < rc2;
                     }
                 }
-                const unsigned m = __ballot_sync(0xffffffffu, hit);
-                if (hit) hits[warp][nh + __popc(m & ((1u << lane) - 1u))] = q;
-                nh += __popc(m);
+                return hit;
+            };
+            // kU candidates per lane per iteration: hits are appended in candidate
+            // order and evaluated 32 at a time
+            const unsigned below = (1u << lane) - 1u;
+            for (int q0 = 0; q0 < ncand; q0 += 32 * kU) {
+                bool hu[kU];
+#pragma unroll
+                for (int v = 0; v < kU; v++) hu[v] = test(q0 + 32 * v + lane);
+#pragma unroll
+                for (int v = 0; v < kU; v++) {
+                    const unsigned mv = __ballot_sync(0xffffffffu, hu[v]);
+                    if (hu[v]) hits[warp][nh + __popc(mv & below)] = q0 + 32 * v + lane;
+                    nh += __popc(mv);
+                }
                 __syncwarp();
-                if (nh >= 32) {
+                while (nh >= 32) {
                     T s0, s1, s2;
                     flush(32, s0, s1, s2);
                     a0.add(s0);
                     a1.add(s1);
                     a2.add(s2);
-                    if (lane < nh - 32) hits[warp][lane] = hits[warp][32 + lane];
-                    nh -= 32;
+                    // the rest (at most 32 kU - 1 entries) moves down by 32
+                    const int rest = nh - 32;
+                    int e[kU];
+#pragma unroll
+                    for (int v = 0; v < kU; v++)
+                        e[v] = lane + 32 * v < rest ? hits[warp][32 + 32 * v + lane] : 0;
+                    __syncwarp();
+#pragma unroll
+                    for (int v = 0; v < kU; v++)
+                        if (lane + 32 * v < rest) hits[warp][32 * v + lane] = e[v];
+                    nh = rest;
                     __syncwarp();
                 }
             }
