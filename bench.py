@@ -275,6 +275,54 @@ def cpu_baseline_batch(systems, nth=None):
             "systems": used, "particles": parts}
 
 
+def host_side_child(args):
+    """Child-process half of host_side: the CPU baseline and/or the FP64 oracle of
+    the first two right-hand sides of synth(w, seed), written to args.host_side."""
+    w = WORKLOADS[args.workload]
+    out = {}
+    if args.workload == "uneven_batch":
+        from spme_gb300.batch import uneven_systems
+        systems = uneven_systems(count=w["count"], xi=w["xi"], rc=w["rc"], radius=w["a"],
+                                 seed=args.host_seed)
+        out["cpu"] = json.dumps(cpu_baseline_batch(systems))
+    else:
+        if not args.no_cpu_baseline:
+            out["cpu"] = json.dumps(cpu_baseline_time(w))
+        if not args.no_oracle_check:
+            import oracle
+            pos, f = synth(w, seed=args.host_seed)
+            nth = os.cpu_count() or 1
+            f2 = f[:2].astype(np.float64)
+            o_rec = oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f2, radius=w["a"],
+                                 nthreads=nth)
+            o_rs = oracle.real_self(pos, w["L"], w["xi"], w["rc"], f2, radius=w["a"],
+                                    nthreads=nth)
+            out["full"], out["real_self"] = o_rec + o_rs, o_rs
+    np.savez(args.host_side, **out)
+    return 0
+
+
+def host_side(workload, seed, want_cpu, want_oracle):
+    """(cpu_baseline, oracle refs) computed in a child process (see host_side_child)."""
+    fd, path = tempfile.mkstemp(suffix=".npz")
+    os.close(fd)
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", workload, "--host-side",
+           path, "--host-seed", str(seed)]
+    if not want_cpu:
+        cmd.append("--no-cpu-baseline")
+    if not want_oracle:
+        cmd.append("--no-oracle-check")
+    try:
+        subprocess.run(cmd, check=True)
+        with np.load(path) as z:
+            cpu = json.loads(str(z["cpu"])) if "cpu" in z.files else None
+            oref = ({"full": z["full"], "real_self": z["real_self"]}
+                    if "full" in z.files else None)
+    finally:
+        os.unlink(path)
+    return cpu, oref
+
+
 def run_reference(args, w):
     """The reference's CPU path on the host cores for the same workload: per step
     one right-hand side of the full system with new positions (the reference's
@@ -352,23 +400,16 @@ def run_gb300(args, w):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    cpu_base = None
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu_base = cpu_baseline_time(w)  # before any GPU work in this process
-
     N, R = w["N"], w["R"]
     pos, f = synth(w, seed=1000 + rank)
-    # FP64 oracle of the first two right-hand sides of the timed inputs (before
-    # any GPU work): reciprocal and real-space + self parts kept apart
-    oref = None
-    if rank == 0 and not args.no_fp64 and not args.no_oracle_check:
-        import oracle
-        nth = os.cpu_count() or 1
-        f2 = f[:2].astype(np.float64)
-        o_rec = oracle.recip(pos, w["L"], w["xi"], w["K"], w["p"], f2, radius=w["a"],
-                             nthreads=nth)
-        o_rs = oracle.real_self(pos, w["L"], w["xi"], w["rc"], f2, radius=w["a"], nthreads=nth)
-        oref = {"full": o_rec + o_rs, "real_self": o_rs}
+    # the CPU baseline and the FP64 oracle of the first two right-hand sides of the
+    # timed inputs run in a child process before any GPU work here, so that their
+    # OpenMP threads and large host arrays never live in the timed process
+    cpu_base, oref = None, None
+    want_cpu = rank == 0 and ws == 1 and not args.no_cpu_baseline
+    want_oracle = rank == 0 and not args.no_fp64 and not args.no_oracle_check
+    if want_cpu or want_oracle:
+        cpu_base, oref = host_side(args.workload, 1000 + rank, want_cpu, want_oracle)
     # a dedicated (non-default) stream: the engine launches on it and the CUDA
     # events below are recorded on it
     stream = torch.cuda.Stream()
@@ -627,7 +668,7 @@ def run_batch(args, w):
     systems = uneven_systems(count=w["count"], xi=w["xi"], rc=w["rc"], radius=w["a"],
                              seed=1234 + rank)
     R = w["R"]
-    cpu_base = (cpu_baseline_batch(systems)
+    cpu_base = (host_side(args.workload, 1234 + rank, True, False)[0]
                 if rank == 0 and ws == 1 and not args.no_cpu_baseline else None)
     rng = np.random.default_rng(77 + rank)
     pos = [torch.tensor(rng.uniform(0, s["L"], (s["N"], 3)), device="cuda") for s in systems]
@@ -709,12 +750,16 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the mid-size and uneven-batch workloads after the large one")
+    ap.add_argument("--host-side", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--host-seed", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--tile", default=None,
                     help="fixed mesh tile 'tx,ty,tz' instead of autotuning (e.g. for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     w = WORKLOADS[args.workload]
+    if args.host_side:
+        return host_side_child(args)
     if args.workload == "uneven_batch":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":
