@@ -396,8 +396,9 @@ struct _spme_batch_t {
     // device
     int *d_sysid = nullptr, *d_pref = nullptr;
     BatchGeo *d_geo = nullptr;
-    int *d_key1 = nullptr, *d_slot1 = nullptr, *d_key2 = nullptr, *d_slot2 = nullptr,
-        *d_key3 = nullptr, *d_slot3 = nullptr;
+    // d_sort_tmp: scratch of the three counting sorts (the atomic slots are kept
+    // in the sorts' permutation buffers until the scatter)
+    int *d_key1 = nullptr, *d_key2 = nullptr, *d_key3 = nullptr, *d_sort_tmp = nullptr;
     int *d_cnt1 = nullptr, *d_off1 = nullptr, *d_cnt2 = nullptr, *d_off2 = nullptr,
         *d_cnt3 = nullptr, *d_off3 = nullptr, *d_scan_tmp = nullptr;
     int *d_perm1 = nullptr, *d_perm2 = nullptr, *d_perm3 = nullptr;
@@ -618,11 +619,9 @@ int create_t(_spme_batch_t *b) {
     BTRY(balloc(&b->d_pref, sizeof(int) * (ns + 1)));
     BTRY(balloc(&b->d_geo, sizeof(BatchGeo) * ns));
     BTRY(balloc(&b->d_key1, sizeof(int) * n));
-    BTRY(balloc(&b->d_slot1, sizeof(int) * n));
     BTRY(balloc(&b->d_key2, sizeof(int) * n));
-    BTRY(balloc(&b->d_slot2, sizeof(int) * n));
     BTRY(balloc(&b->d_key3, sizeof(int) * n));
-    BTRY(balloc(&b->d_slot3, sizeof(int) * n));
+    BTRY(balloc(&b->d_sort_tmp, sizeof(int) * n));
     BTRY(balloc(&b->d_cnt2, sizeof(int) * start));
     BTRY(balloc(&b->d_off2, sizeof(int) * (start + 1)));
     BTRY(balloc(&b->d_cnt3, sizeof(int) * cell));
@@ -796,15 +795,15 @@ int positions_body(_spme_batch_t *b, const double *pos) {
     BTRY_CUDA(cudaMemsetAsync(b->d_cnt2, 0, sizeof(int) * b->nstart_keys, s));
     BTRY_CUDA(cudaMemsetAsync(b->d_cnt3, 0, sizeof(int) * b->ncell_keys, s));
     k_batch_keys<T><<<nblk(n, 256), 256, 0, s>>>(
-        pos, n, b->d_sysid, b->d_geo, b->d_key1, b->d_cnt1, b->d_slot1, b->d_key2, b->d_cnt2,
-        b->d_slot2, b->d_key3, b->d_cnt3, b->d_slot3, b->d_pstart, (T *)b->d_pfrac,
+        pos, n, b->d_sysid, b->d_geo, b->d_key1, b->d_cnt1, b->d_perm1, b->d_key2, b->d_cnt2,
+        b->d_perm2, b->d_key3, b->d_cnt3, b->d_perm3, b->d_pstart, (T *)b->d_pfrac,
         (typename V4T<T>::type *)b->d_prel);
     launch_scan(b->d_cnt1, b->ntile_keys, b->d_off1, b->d_scan_tmp, s);
-    launch_scatter(b->d_key1, b->d_slot1, b->d_off1, n, b->d_perm1, s);
+    launch_scatter(b->d_key1, b->d_off1, n, b->d_perm1, b->d_sort_tmp, s);
     launch_scan(b->d_cnt2, b->nstart_keys, b->d_off2, b->d_scan_tmp, s);
-    launch_scatter(b->d_key2, b->d_slot2, b->d_off2, n, b->d_perm2, s);
+    launch_scatter(b->d_key2, b->d_off2, n, b->d_perm2, b->d_sort_tmp, s);
     launch_scan(b->d_cnt3, b->ncell_keys, b->d_off3, b->d_scan_tmp, s);
-    launch_scatter(b->d_key3, b->d_slot3, b->d_off3, n, b->d_perm3, s);
+    launch_scatter(b->d_key3, b->d_off3, n, b->d_perm3, b->d_sort_tmp, s);
     k_batch_records<T><<<nblk(n, kRecThreads), kRecThreads, 0, s>>>(b->d_pstart, (const T *)b->d_pfrac,
                                                     b->d_perm1, n, b->d_sysid, b->d_geo, b->ws,
                                                     b->d_ridx1, b->d_rst1, (T *)b->d_rw1);
@@ -812,7 +811,7 @@ int positions_body(_spme_batch_t *b, const double *pos) {
                                                     b->d_perm2, n, b->d_sysid, b->d_geo, b->ws,
                                                     b->d_ridx2, b->d_rst2, (T *)b->d_rw2);
     launch_cell_gather(b->d_prel, b->d_perm3, n, sizeof(T) == 4, b->d_cpos, s);
-    b->launches += 1 + 3 * 3 + 3 + 2 + 1;
+    b->launches += 1 + 3 * 3 + 3 * 2 + 2 + 1;
     return from_cuda(cudaGetLastError());
 }
 
@@ -932,8 +931,8 @@ void destroy_b(_spme_batch_t *b) {
         if (g.fwd) cufftDestroy(g.fwd);
         if (g.bwd) cufftDestroy(g.bwd);
     }
-    void *bufs[] = {b->d_sysid, b->d_pref,  b->d_geo,   b->d_key1,  b->d_slot1, b->d_key2,
-                    b->d_slot2, b->d_key3,  b->d_slot3, b->d_cnt1,  b->d_off1,  b->d_cnt2,
+    void *bufs[] = {b->d_sysid, b->d_pref,  b->d_geo,   b->d_key1,  b->d_key2,
+                    b->d_key3,  b->d_sort_tmp, b->d_cnt1,  b->d_off1,  b->d_cnt2,
                     b->d_off2,  b->d_cnt3,  b->d_off3,  b->d_scan_tmp, b->d_perm1, b->d_perm2,
                     b->d_perm3, b->d_pstart, b->d_pfrac, b->d_prel, b->d_cpos,  b->d_ridx1,
                     b->d_ridx2, b->d_rst1,  b->d_rst2,  b->d_rw1,   b->d_rw2,   b->d_F,

@@ -125,10 +125,12 @@ struct _spme_t {
     bool have_pos = false;
     // device buffers
     double *d_pos = nullptr;
-    int *d_key2 = nullptr, *d_slot2 = nullptr, *d_key3 = nullptr, *d_slot3 = nullptr;
+    int *d_key2 = nullptr, *d_key3 = nullptr;
     uint32_t *d_pstart = nullptr;  // per-particle stencil start (mesh engines)
     void *d_pfrac = nullptr;       // per-particle fractional mesh coordinates
-    int *d_key = nullptr, *d_slot = nullptr, *d_tcount = nullptr, *d_toff = nullptr,
+    // d_sort_tmp: scratch of the three counting sorts (the atomic slots are kept
+    // in the sorts' permutation buffers until the scatter)
+    int *d_key = nullptr, *d_sort_tmp = nullptr, *d_tcount = nullptr, *d_toff = nullptr,
         *d_tperm = nullptr, *d_scan_tmp = nullptr;
     int *d_rec_idx = nullptr;
     uint32_t *d_rec_start = nullptr;
@@ -474,9 +476,8 @@ int create_impl(const spme_params &prm, spme_t **out) {
     const size_t C = (size_t)e->Cmax;
     TRY(dalloc(&e->d_pos, sizeof(double) * 3 * n));
     TRY(dalloc(&e->d_key, sizeof(int) * n));
-    TRY(dalloc(&e->d_slot, sizeof(int) * n));
+    TRY(dalloc(&e->d_sort_tmp, sizeof(int) * n));
     TRY(dalloc(&e->d_key3, sizeof(int) * n));
-    TRY(dalloc(&e->d_slot3, sizeof(int) * n));
     TRY(dalloc(&e->d_tperm, sizeof(int) * n));
     if (prm.terms & SPME_TERM_RECIP) {
         TRY(dalloc(&e->d_pstart, sizeof(uint32_t) * n));
@@ -489,7 +490,6 @@ int create_impl(const spme_params &prm, spme_t **out) {
         TRY(dalloc(&e->d_soff, sizeof(int) * (K3 + 1)));
         TRY(dalloc(&e->d_sperm, sizeof(int) * n));
         TRY(dalloc(&e->d_key2, sizeof(int) * n));
-        TRY(dalloc(&e->d_slot2, sizeof(int) * n));
         TRY(dalloc(&e->d_srec_idx, sizeof(int) * n));
         TRY(dalloc(&e->d_srec_start, sizeof(uint32_t) * n));
         TRY(dalloc(&e->d_srec_w, e->elem * record_width(e) * n));
@@ -650,14 +650,14 @@ void destroy_impl(spme_t *e) {
             cufftDestroy(p.bwd2);
         }
     }
-    void *bufs[] = {e->d_pos,    e->d_key,     e->d_slot,  e->d_tcount,   e->d_toff,
+    void *bufs[] = {e->d_pos,    e->d_key,     e->d_sort_tmp, e->d_tcount,   e->d_toff,
                     e->d_tperm,  e->d_scan_tmp, e->d_rec_idx, e->d_rec_start, e->d_rec_w,
                     e->d_ccount, e->d_coff,    e->d_cperm, e->d_cpos,     e->d_prel, e->d_mesh,
                     e->d_cmesh,  e->d_tab,     e->d_bmod2, e->d_work,     e->d_F,
                     e->d_W,      e->d_fstage,  e->d_ustage, e->d_err,  e->d_ztw,
                     e->d_zip,    e->d_f2tab,    e->d_scount,  e->d_soff,   e->d_sperm, e->d_srec_idx,
                     e->d_srec_start, e->d_srec_w, e->d_Fs, e->d_W2, e->d_pair, e->d_key2,
-                    e->d_slot2,  e->d_key3,   e->d_slot3, e->d_pstart, e->d_pfrac};
+                    e->d_key3,   e->d_pstart, e->d_pfrac};
     for (void *b : bufs) dfree(b);
     for (int i = 0; i <= kStages; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -699,15 +699,15 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
     if (recip || real) {
         // one pass over the positions for every key this engine sorts by
         spme::launch_all_keys(e->d_pos, n, e->g, e->nc, e->d_key, recip ? e->d_tcount : nullptr,
-                              e->d_slot, e->d_key2, cols ? e->d_scount : nullptr, e->d_slot2,
-                              e->d_key3, real ? e->d_ccount : nullptr, e->d_slot3,
+                              e->d_tperm, e->d_key2, cols ? e->d_scount : nullptr, e->d_sperm,
+                              e->d_key3, real ? e->d_ccount : nullptr, e->d_cperm,
                               recip ? e->d_pstart : nullptr, e->d_pfrac,
                               real ? e->d_prel : nullptr, is_fp32(e), s);
         e->launches++;
     }
     if (recip) {
         spme::launch_scan(e->d_tcount, e->ntiles, e->d_toff, e->d_scan_tmp, s);
-        spme::launch_scatter(e->d_key, e->d_slot, e->d_toff, n, e->d_tperm, s);
+        spme::launch_scatter(e->d_key, e->d_toff, n, e->d_tperm, e->d_sort_tmp, s);
         if (is_fp32(e))
             spme::launch_records<float>(e->d_pstart, (const float *)e->d_pfrac, e->d_tperm, n,
                                         e->g.p, e->d_rec_idx, e->d_rec_start,
@@ -716,11 +716,11 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
             spme::launch_records<double>(e->d_pstart, (const double *)e->d_pfrac, e->d_tperm, n,
                                          e->g.p, e->d_rec_idx, e->d_rec_start,
                                          (double *)e->d_rec_w, s);
-        e->launches += 5;
+        e->launches += 6;
     }
     if (cols) {
         spme::launch_scan(e->d_scount, K3, e->d_soff, e->d_scan_tmp, s);
-        spme::launch_scatter(e->d_key2, e->d_slot2, e->d_soff, n, e->d_sperm, s);
+        spme::launch_scatter(e->d_key2, e->d_soff, n, e->d_sperm, e->d_sort_tmp, s);
         if (is_fp32(e))
             spme::launch_records<float>(e->d_pstart, (const float *)e->d_pfrac, e->d_sperm, n,
                                         e->g.p, e->d_srec_idx, e->d_srec_start,
@@ -729,13 +729,13 @@ int set_positions_body(spme_t *e, const double *pos, int mem) {
             spme::launch_records<double>(e->d_pstart, (const double *)e->d_pfrac, e->d_sperm, n,
                                          e->g.p, e->d_srec_idx, e->d_srec_start,
                                          (double *)e->d_srec_w, s);
-        e->launches += 5;
+        e->launches += 6;
     }
     if (real) {
         spme::launch_scan(e->d_ccount, ncell, e->d_coff, e->d_scan_tmp, s);
-        spme::launch_scatter(e->d_key3, e->d_slot3, e->d_coff, n, e->d_cperm, s);
+        spme::launch_scatter(e->d_key3, e->d_coff, n, e->d_cperm, e->d_sort_tmp, s);
         spme::launch_cell_gather(e->d_prel, e->d_cperm, n, is_fp32(e), e->d_cpos, s);
-        e->launches += 5;
+        e->launches += 6;
     }
     TRY_CUDA(cudaGetLastError());
     return SPME_OK;

@@ -34,8 +34,10 @@ void launch_cell_keys(const double *pos, int n, double L, int nc, int *key, int 
 // tmp must hold scan_tmp_elems(nkeys) ints.
 size_t scan_tmp_elems(int nkeys);
 void launch_scan(const int *count, int nkeys, int *off, int *tmp, cudaStream_t s);
-// perm[off[key[i]] + slot[i]] = i
-void launch_scatter(const int *key, const int *slot, const int *off, int n, int *perm,
+// Counting-sort scatter.  On entry perm[i] is particle i's slot within its key
+// (from the atomic counts, in no fixed order); on return perm[off[k] ..
+// off[k + 1]) lists key k's particles in increasing index.  tmp: n ints.
+void launch_scatter(const int *key, const int *off, int n, int *perm, int *tmp,
                     cudaStream_t s);
 // B-spline records in sorted order (perm): rec_idx[s] = perm[s], the packed
 // stencil start, and p weights per axis (record width RecordWidth<T,P>), from

@@ -114,9 +114,9 @@ extern "C" int spme_realspace_apply_noalloc(int np, const double *pos, double bo
         cudaGetLastError();
         return SPME_ERR_CUDA;
     }
-    spme::launch_cell_keys(pos, np, box_size, (int)nc, key, count, slot, s);
+    spme::launch_cell_keys(pos, np, box_size, (int)nc, key, count, perm, s);
     spme::launch_scan(count, ncell, off, tmp, s);
-    spme::launch_scatter(key, slot, off, np, perm, s);
+    spme::launch_scatter(key, off, np, perm, slot, s);
     spme::launch_cell_positions(pos, perm, np, box_size, (int)nc, false, cpos, s);
     spme::launch_pack<double>(f, ldf, np, nrhs, F, s);
     if (spme::launch_realspace<double>((int)nc, off, perm, cpos, F, nrhs, box_size, rcut, xi,

@@ -190,6 +190,30 @@ __global__ void k_scatter(const int *__restrict__ key, const int *__restrict__ s
     perm[off[key[i]] + slot[i]] = i;
 }
 
+// Keys holding more particles than this keep the order of the atomic slots:
+// ranking a key's particles costs (its count)^2 / 32 warp steps.
+constexpr int kStableMax = 16384;
+
+// Particle v = in[q] goes to out[b + r], r its rank by particle index among
+// the particles of its key [b, e): every key's particles in increasing index,
+// so a position build gives the same order (and the sums over particles the
+// same rounding) on every run.  Consecutive q share a key, so the lanes of a
+// warp read the same entries (broadcast loads).
+__global__ void k_stable_place(const int *__restrict__ key, const int *__restrict__ off,
+                               const int *__restrict__ in, int n, int *__restrict__ out) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int v = in[q];
+    const int k = key[v];
+    const int b = off[k], e = off[k + 1];
+    int r = q - b;
+    if (e - b <= kStableMax) {
+        r = 0;
+        for (int j = b; j < e; j++) r += in[j] < v;
+    }
+    out[b + r] = v;
+}
+
 // The block's records are assembled in shared memory and written as one
 // contiguous run of 16-byte stores: a record is WS elements (80 bytes at p = 6
 // FP32), and per-thread record stores would touch a separate sector per lane.
@@ -306,9 +330,11 @@ void launch_scan(const int *count, int nkeys, int *off, int *tmp, cudaStream_t s
     k_scan_final<<<nb, kScanThreads, 0, s>>>(count, nkeys, tmp, off);
 }
 
-void launch_scatter(const int *key, const int *slot, const int *off, int n, int *perm,
+void launch_scatter(const int *key, const int *off, int n, int *perm, int *tmp,
                     cudaStream_t s) {
-    if (n > 0) k_scatter<<<nblk(n, 256), 256, 0, s>>>(key, slot, off, n, perm);
+    if (n <= 0) return;
+    k_scatter<<<nblk(n, 256), 256, 0, s>>>(key, perm, off, n, tmp);
+    k_stable_place<<<nblk(n, 256), 256, 0, s>>>(key, off, tmp, n, perm);
 }
 
 template <typename T>
