@@ -10,9 +10,11 @@
 //     (bounded wait, error flag on timeout); for tiles whose halo wraps the
 //     periodic boundary the part past K arrives as zeros and is patched with
 //     16-byte vector loads (all rows with plain loads when TMA is unavailable).
-// Each warp then interpolates the tile's own particles (sorted by stencil
-// start) from shared memory: lanes are (x offset 0..7, component 0..3)
-// pairs, the x offsets summed with shuffles.  Every particle is handled by
+// Each warp then interpolates the tile's own particles from shared memory:
+// FP32 at p = 4, 6 two particles per warp with lanes = (x column pair,
+// component) and two-lane FMAs (interp_pairs); otherwise one particle per warp
+// with lanes = (x offset 0..7, component 0..3).  The x offsets are summed with
+// shuffles.  Every particle is handled by
 // exactly one CTA; mesh values come from HBM about once and from L2 for the
 // halos.
 #include <algorithm>
@@ -30,6 +32,78 @@ constexpr int kHX = 24;  // staged row width (elements)
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+// P consecutive record weights starting at w (16-byte aligned record, offset
+// P: 8-byte aligned for P = 6, 16-byte for P = 4) as vector loads.
+template <int P>
+__device__ __forceinline__ void load_weights(const float *w, float (&out)[P]) {
+    if constexpr (P == 4) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(w));
+        out[0] = v.x, out[1] = v.y, out[2] = v.z, out[3] = v.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < P; k += 2) {
+            const float2 v = __ldg(reinterpret_cast<const float2 *>(w + k));
+            out[k] = v.x, out[k + 1] = v.y;
+        }
+    }
+}
+
+// FP32, 4-component boxes, p = 4 or 6: two particles per warp, one per
+// half-warp, lanes of a half = (x pair 0..3, component 0..3).  A lane's x pair
+// starts at an even box column (the particle's first column, or the one before
+// it when that is odd), is read with one 8-byte load and meets its two x
+// weights (times the y weight) in one two-lane FMA (fma.rn.f32x2): each load
+// and FMA instruction covers two mesh points.  Columns outside the stencil
+// carry zero weights (the box is 24 columns wide: a pair ends at most at
+// column tx + 6).
+template <int P>
+__device__ __forceinline__ void interp_pairs(const float *box, int PS, int HYB,
+                                             const InterpArgs<float> &A, int c0, int nc,
+                                             int pbeg, int pend, int ox, int oy, int oz) {
+    constexpr int kWarps = kThreads / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int h = lane >> 4, xp = (lane >> 2) & 3, cl = lane & 3;
+    const int WS = A.ws, C = A.C;
+    for (int s0 = pbeg + 2 * warp; s0 < pend; s0 += 2 * kWarps) {
+        const int s = s0 + h;
+        const bool have = s < pend;
+        const int sr = have ? s : s0;  // the idle half reads a valid record
+        const float *rw = A.rec_w + (size_t)sr * WS;
+        int sx, sy, sz;
+        unpack_start(__ldg(A.rec_start + sr), sx, sy, sz);
+        const int lx = sx - ox, ly = sy - oy, lz = sz - oz;  // own tile: no wrap
+        const int odd = lx & 1;
+        const int i0 = 2 * xp - odd;  // stencil column of the pair's first point
+        const float wx0 = (i0 >= 0 && i0 < P) ? __ldg(rw + i0) : 0.f;
+        const float wx1 = i0 + 1 < P ? __ldg(rw + i0 + 1) : 0.f;
+        float wy[P], wz[P];
+        load_weights<P>(rw + P, wy);
+        load_weights<P>(rw + 2 * P, wz);
+        float2 wxy[P];
+#pragma unroll
+        for (int y = 0; y < P; y++) wxy[y] = make_float2(wx0 * wy[y], wx1 * wy[y]);
+        const float *base = box + (size_t)cl * PS + (lz * HYB + ly) * kHX + (lx - odd) + 2 * xp;
+        float2 acc = make_float2(0.f, 0.f);
+        // sum over y with w_x w_y first, then one w_z per plane
+#pragma unroll
+        for (int z = 0; z < P; z++) {
+            const float *pz = base + z * HYB * kHX;
+            float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int y = 0; y < P; y++)
+                t = __ffma2_rn(wxy[y], *reinterpret_cast<const float2 *>(pz + y * kHX), t);
+            acc = __ffma2_rn(make_float2(wz[z], wz[z]), t, acc);
+        }
+        float a = acc.x + acc.y;
+        a += __shfl_xor_sync(0xffffffffu, a, 4);
+        a += __shfl_xor_sync(0xffffffffu, a, 8);
+        if (have && xp == 0 && cl < nc) {
+            float *out = A.W + (size_t)__ldg(A.rec_idx + s) * C + c0 + cl;
+            *out = A.accumulate ? *out + a : a;
+        }
+    }
+}
 
 // One tile's work (the body of the single-system kernel and of the batched
 // one); tmap is read only when use_tma is set.
@@ -114,13 +188,15 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
         __syncthreads();
     };
 
+    // FP32 p = 4, 6: two particles per warp, x columns in pairs (interp_pairs)
+    constexpr bool kPairs = sizeof(T) == 4 && CG == 4 && (P == 4 || P == 6);
     // the warp's first particle's record, the same for every component chunk:
     // loaded once, before the first box is waited for
     constexpr int kWarps = kThreads / 32;
     T wreg_0 = T(0);
     uint32_t st_0 = 0;
     int idx_0 = 0;
-    if (pbeg + warp < pend) {
+    if (!kPairs && pbeg + warp < pend) {
         const int s = pbeg + warp;
         wreg_0 = lane < 3 * P ? __ldg(rec_w + (size_t)s * WS + lane) : T(0);
         st_0 = __ldg(rec_start + s);
@@ -144,6 +220,13 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
             if (wraps) stage_rows(c0, nc, true);
         } else {
             stage_rows(c0, nc, false);
+        }
+        if constexpr (kPairs) {
+            interp_pairs<P>(reinterpret_cast<const float *>(box), PS, HYB,
+                            reinterpret_cast<const InterpArgs<float> &>(A), c0, nc, pbeg, pend,
+                            ox, oy, oz);
+            __syncthreads();  // the box is rewritten by the next chunk
+            continue;
         }
         // the next particle's record is loaded while this one is interpolated
         T wreg_n = wreg_0;
