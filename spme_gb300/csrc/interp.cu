@@ -33,20 +33,23 @@ template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
 template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
 
-// P consecutive record weights starting at w (16-byte aligned record, offset
-// P: 8-byte aligned for P = 6, 16-byte for P = 4) as vector loads.
+// A half-warp's copy of one particle record for interp_pairs: lane j of the
+// half holds weights j and 16 + j (the record's 3p weights: x, y, z), plus
+// the stencil start; read by shuffles within the half.
+struct HalfRec {
+    float wa, wb;
+    uint32_t st;
+};
+
 template <int P>
-__device__ __forceinline__ void load_weights(const float *w, float (&out)[P]) {
-    if constexpr (P == 4) {
-        const float4 v = __ldg(reinterpret_cast<const float4 *>(w));
-        out[0] = v.x, out[1] = v.y, out[2] = v.z, out[3] = v.w;
-    } else {
-#pragma unroll
-        for (int k = 0; k < P; k += 2) {
-            const float2 v = __ldg(reinterpret_cast<const float2 *>(w + k));
-            out[k] = v.x, out[k + 1] = v.y;
-        }
-    }
+__device__ __forceinline__ HalfRec load_pair_rec(const InterpArgs<float> &A, int s) {
+    const int j = threadIdx.x & 15;
+    const float *rw = A.rec_w + (size_t)s * A.ws;
+    HalfRec r;
+    r.wa = j < 3 * P ? __ldg(rw + j) : 0.f;
+    r.wb = j < 3 * P - 16 ? __ldg(rw + 16 + j) : 0.f;
+    r.st = __ldg(A.rec_start + s);
+    return r;
 }
 
 // FP32, 4-component boxes, p = 4 or 6: two particles per warp, one per
@@ -56,33 +59,45 @@ __device__ __forceinline__ void load_weights(const float *w, float (&out)[P]) {
 // weights (times the y weight) in one two-lane FMA (fma.rn.f32x2): each load
 // and FMA instruction covers two mesh points.  Columns outside the stencil
 // carry zero weights (the box is 24 columns wide: a pair ends at most at
-// column tx + 6).
+// column tx + 6).  The next pair's records are loaded while this pair is
+// interpolated; rec0 is the warp's first pair, loaded once per tile.
 template <int P>
 __device__ __forceinline__ void interp_pairs(const float *box, int PS, int HYB,
                                              const InterpArgs<float> &A, int c0, int nc,
-                                             int pbeg, int pend, int ox, int oy, int oz) {
+                                             int pbeg, int pend, int ox, int oy, int oz,
+                                             HalfRec rec0) {
     constexpr int kWarps = kThreads / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int h = lane >> 4, xp = (lane >> 2) & 3, cl = lane & 3;
-    const int WS = A.ws, C = A.C;
+    const int C = A.C;
+    HalfRec nxt = rec0;
     for (int s0 = pbeg + 2 * warp; s0 < pend; s0 += 2 * kWarps) {
+        const HalfRec r = nxt;
+        if (s0 + 2 * kWarps < pend) nxt = load_pair_rec<P>(A, min(s0 + 2 * kWarps + h, pend - 1));
+        // weight i of this half's particle
+        auto w = [&](int i) {
+            return i < 16 ? __shfl_sync(0xffffffffu, r.wa, i, 16)
+                          : __shfl_sync(0xffffffffu, r.wb, i - 16, 16);
+        };
         const int s = s0 + h;
-        const bool have = s < pend;
-        const int sr = have ? s : s0;  // the idle half reads a valid record
-        const float *rw = A.rec_w + (size_t)sr * WS;
         int sx, sy, sz;
-        unpack_start(__ldg(A.rec_start + sr), sx, sy, sz);
+        unpack_start(r.st, sx, sy, sz);
         const int lx = sx - ox, ly = sy - oy, lz = sz - oz;  // own tile: no wrap
         const int odd = lx & 1;
         const int i0 = 2 * xp - odd;  // stencil column of the pair's first point
-        const float wx0 = (i0 >= 0 && i0 < P) ? __ldg(rw + i0) : 0.f;
-        const float wx1 = i0 + 1 < P ? __ldg(rw + i0 + 1) : 0.f;
-        float wy[P], wz[P];
-        load_weights<P>(rw + P, wy);
-        load_weights<P>(rw + 2 * P, wz);
+        const float x0 = __shfl_sync(0xffffffffu, r.wa, i0 & 15, 16);
+        const float x1 = __shfl_sync(0xffffffffu, r.wa, i0 + 1, 16);
+        const float wx0 = i0 >= 0 && i0 < P ? x0 : 0.f;
+        const float wx1 = i0 + 1 < P ? x1 : 0.f;
         float2 wxy[P];
+        float wz[P];
 #pragma unroll
-        for (int y = 0; y < P; y++) wxy[y] = make_float2(wx0 * wy[y], wx1 * wy[y]);
+        for (int y = 0; y < P; y++) {
+            const float wy = w(P + y);
+            wxy[y] = make_float2(wx0 * wy, wx1 * wy);
+        }
+#pragma unroll
+        for (int z = 0; z < P; z++) wz[z] = w(2 * P + z);
         const float *base = box + (size_t)cl * PS + (lz * HYB + ly) * kHX + (lx - odd) + 2 * xp;
         float2 acc = make_float2(0.f, 0.f);
         // sum over y with w_x w_y first, then one w_z per plane
@@ -98,7 +113,7 @@ __device__ __forceinline__ void interp_pairs(const float *box, int PS, int HYB,
         float a = acc.x + acc.y;
         a += __shfl_xor_sync(0xffffffffu, a, 4);
         a += __shfl_xor_sync(0xffffffffu, a, 8);
-        if (have && xp == 0 && cl < nc) {
+        if (s < pend && xp == 0 && cl < nc) {
             float *out = A.W + (size_t)__ldg(A.rec_idx + s) * C + c0 + cl;
             *out = A.accumulate ? *out + a : a;
         }
@@ -196,7 +211,12 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
     T wreg_0 = T(0);
     uint32_t st_0 = 0;
     int idx_0 = 0;
-    if (!kPairs && pbeg + warp < pend) {
+    HalfRec hrec_0{0.f, 0.f, 0u};
+    if constexpr (kPairs) {
+        if (pbeg + 2 * warp < pend)
+            hrec_0 = load_pair_rec<P>(reinterpret_cast<const InterpArgs<float> &>(A),
+                                      min(pbeg + 2 * warp + (lane >> 4), pend - 1));
+    } else if (pbeg + warp < pend) {
         const int s = pbeg + warp;
         wreg_0 = lane < 3 * P ? __ldg(rec_w + (size_t)s * WS + lane) : T(0);
         st_0 = __ldg(rec_start + s);
@@ -224,7 +244,7 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
         if constexpr (kPairs) {
             interp_pairs<P>(reinterpret_cast<const float *>(box), PS, HYB,
                             reinterpret_cast<const InterpArgs<float> &>(A), c0, nc, pbeg, pend,
-                            ox, oy, oz);
+                            ox, oy, oz, hrec_0);
             __syncthreads();  // the box is rewritten by the next chunk
             continue;
         }
