@@ -205,6 +205,43 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
 
     // FP32 p = 4, 6: two particles per warp, x columns in pairs (interp_pairs)
     constexpr bool kPairs = sizeof(T) == 4 && CG == 4 && (P == 4 || P == 6);
+    // after a TMA box of a tile whose halo wraps: the elements past the periodic
+    // boundary (zeros in the box) from plain loads, one thread per box row: a
+    // row past K in y or z is copied whole, other rows only from column K - ox on
+    const int xw0 = ox + hx > K ? (K - ox) / VW : NV;  // first vector holding a wrapped column
+    const int xw1 = (hx - 1) / VW;                     // last vector of the halo
+    auto patch_wrapped = [&](int c0, int nc) {
+        const bool vec = (K % VW) == 0 && (ox % VW) == 0;
+        DivMod dhy, dhz;
+        dhy.init(hy);
+        dhz.init(hz);
+        const int nrow = nc * hz * hy;
+        for (int row = threadIdx.x; row < nrow; row += kThreads) {
+            int y, z;
+            const int cz = dhy.div(row, y);
+            const int c = dhz.div(cz, z);
+            int gy = oy + y, gz = oz + z;
+            const bool row_wraps = gy >= K || gz >= K;
+            if (!row_wraps && xw0 == NV) continue;
+            gy -= gy >= K ? K : 0;
+            gz -= gz >= K ? K : 0;
+            const T *src = mesh + (size_t)(c0 + c) * K3 + (size_t)gz * K2 + (size_t)gy * K;
+            T *dst = box + (size_t)c * PS + (z * HYB + y) * kHX;
+            const int v1 = row_wraps ? NV - 1 : xw1;
+            for (int v = row_wraps ? 0 : xw0; v <= v1; v++) {
+                const int x0 = ox + v * VW;
+                if (vec) {
+                    *reinterpret_cast<V *>(dst + v * VW) =
+                        __ldg(reinterpret_cast<const V *>(src + x0 % K));
+                } else {
+#pragma unroll
+                    for (int e = 0; e < VW; e++) dst[v * VW + e] = __ldg(src + (x0 + e) % K);
+                }
+            }
+        }
+        __syncthreads();
+    };
+
     // the warp's first particle's record, the same for every component chunk:
     // loaded once, before the first box is waited for
     constexpr int kWarps = kThreads / 32;
@@ -237,7 +274,7 @@ __device__ __forceinline__ void interp_body(const CUtensorMap *tmap, const Inter
                 if (threadIdx.x == 0) atomicExch(err, 1);
                 return;
             }
-            if (wraps) stage_rows(c0, nc, true);
+            if (wraps) patch_wrapped(c0, nc);
         } else {
             stage_rows(c0, nc, false);
         }
@@ -311,7 +348,11 @@ template <typename T, int P, int CG>
 // blocks per SM that the 4-component box's shared memory allows (16x8x4 tiles)
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 5 : 2)
 k_interp(const __grid_constant__ CUtensorMap tmap, InterpArgs<T> A) {
-    interp_body<T, P, CG>(&tmap, A, blockIdx.x);
+    // tiles z fastest: blocks launched together are z neighbours, whose boxes
+    // share p - 1 of their tz + p - 1 planes (read from L2 by the later ones)
+    const int b = blockIdx.x, ntx = A.g.ntx, nty = A.g.nty, ntz = A.g.ntz;
+    const int tiz = b % ntz, rest = b / ntz;
+    interp_body<T, P, CG>(&tmap, A, (tiz * nty + rest / ntx) * ntx + rest % ntx);
 }
 
 // Many systems in one persistent launch over their tiles: each system's boxes
