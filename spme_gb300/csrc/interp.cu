@@ -3,9 +3,9 @@
 //
 // One CTA per mesh tile.  For CG components at a time it stages the tile
 // plus its (p-1) upper halo in shared memory as a dense box
-// [CG][HZB][HYB][HX] (HX = 24 wide: every lane's x offset fits, and the
-// component-plane stride is 24 (mod 32) words so the gather below is
-// bank-conflict free):
+// [CG][HZB][HYB][HX] (HX = 24 wide: every lane's x offset fits; at 16x8x4
+// tiles the component-plane stride is 24 (mod 32) words, so the gather below
+// is bank-conflict free):
 //   * one TMA (cp.async.bulk.tensor) load per chunk, completing on an mbarrier
 //     (bounded wait, error flag on timeout); for tiles whose halo wraps the
 //     periodic boundary the part past K arrives as zeros and is patched with
@@ -14,9 +14,8 @@
 // FP32 at p = 4, 6 two particles per warp with lanes = (x column pair,
 // component) and two-lane FMAs (interp_pairs); otherwise one particle per warp
 // with lanes = (x offset 0..7, component 0..3).  The x offsets are summed with
-// shuffles.  Every particle is handled by
-// exactly one CTA; mesh values come from HBM about once and from L2 for the
-// halos.
+// shuffles.  Every particle is handled by exactly one CTA; a tile's halo is
+// staged again by its neighbours (from L2 where it is still cached).
 #include <algorithm>
 
 #include "kernels.h"
